@@ -1,0 +1,614 @@
+// abi.cu -- the extern "C" entry points of include/dfs_gb300.h: argument
+// validation (the reference's assert()s, src/distributed_statevector.hpp:191,
+// src/distributed_densitymatrix.hpp:16,80,352, become status codes), state
+// ownership, the single-rank environment and the density-matrix wrappers of
+// src/distributed_densitymatrix.hpp:15-89 composed from statevector sweeps.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "engine.hpp"
+
+namespace dfs {
+
+// ------------------------------------------------------------- errors
+
+static thread_local char g_lastError[512] = "";
+
+int fail(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_lastError, sizeof g_lastError, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int cuda_fail(cudaError_t err, const char* what) {
+    cudaGetLastError();  // clear sticky-free errors so the context stays usable
+    if (err == cudaErrorMemoryAllocation) return fail(DFS_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(err));
+    return fail(DFS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(err));
+}
+
+// ------------------------------------------------------------ context
+
+static Context g_ctx;
+static std::mutex g_initMutex;
+
+Context& ctx() { return g_ctx; }
+
+static int ensure_init() {
+    if (g_ctx.initialised) return DFS_SUCCESS;
+    std::lock_guard<std::mutex> lock(g_initMutex);
+    if (g_ctx.initialised) return DFS_SUCCESS;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    cudaDeviceProp p;
+    e = cudaGetDeviceProperties(&p, dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceProperties");
+    g_ctx.device = dev;
+    g_ctx.numSMs = p.multiProcessorCount;
+    g_ctx.smemOptin = p.sharedMemPerBlockOptin;
+    e = cudaStreamCreateWithFlags(&g_ctx.ownStream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
+    g_ctx.stream = g_ctx.ownStream;
+    e = cudaEventCreateWithFlags(&g_ctx.pinnedFree, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+    g_ctx.initialised = true;
+    return DFS_SUCCESS;
+}
+
+void* scratch(size_t bytes) {
+    if (bytes <= g_ctx.scratchBytes) return g_ctx.scratch;
+    size_t want = std::max<size_t>(bytes, 1 << 20);
+    if (g_ctx.scratch) {
+        cudaStreamSynchronize(g_ctx.stream);
+        cudaFree(g_ctx.scratch);
+        g_ctx.scratch = nullptr;
+        g_ctx.scratchBytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&g_ctx.scratch, want);
+    if (e != cudaSuccess) {
+        g_ctx.scratch = nullptr;
+        cuda_fail(e, "scratch allocation");
+        return nullptr;
+    }
+    g_ctx.scratchBytes = want;
+    return g_ctx.scratch;
+}
+
+int upload_scratch(const void* host, size_t bytes, size_t offset) {
+    if (!scratch(offset + bytes)) return DFS_ERR_OUT_OF_MEMORY;
+    // the previous staged upload must have left the pinned buffer
+    cudaError_t e = cudaEventSynchronize(g_ctx.pinnedFree);
+    if (e != cudaSuccess) return cuda_fail(e, "staging wait");
+    if (bytes > g_ctx.pinnedBytes) {
+        if (g_ctx.pinned) cudaFreeHost(g_ctx.pinned);
+        size_t want = std::max<size_t>(bytes, 1 << 16);
+        e = cudaMallocHost(&g_ctx.pinned, want);
+        if (e != cudaSuccess) {
+            g_ctx.pinned = nullptr;
+            g_ctx.pinnedBytes = 0;
+            return cuda_fail(e, "pinned staging allocation");
+        }
+        g_ctx.pinnedBytes = want;
+    }
+    memcpy(g_ctx.pinned, host, bytes);
+    e = cudaMemcpyAsync((char*)g_ctx.scratch + offset, g_ctx.pinned, bytes, cudaMemcpyHostToDevice, g_ctx.stream);
+    if (e == cudaSuccess) e = cudaEventRecord(g_ctx.pinnedFree, g_ctx.stream);
+    return e == cudaSuccess ? DFS_SUCCESS : cuda_fail(e, "scratch upload");
+}
+
+// ----------------------------------------------------------- validation
+
+static int check_state(dfs_state s) {
+    if (!s) return fail(DFS_ERR_INVALID_ARG, "null state handle");
+    return ensure_init();
+}
+
+static int check_dm(dfs_state s) {
+    int rc = check_state(s);
+    if (rc) return rc;
+    if (!s->isDM) return fail(DFS_ERR_STATE_KIND, "a density matrix is required");
+    return DFS_SUCCESS;
+}
+
+static int check_qubit(unsigned q, unsigned bound, const char* what) {
+    if (q >= bound) return fail(DFS_ERR_QUBIT_INDEX, "%s %u is not below %u", what, q, bound);
+    return DFS_SUCCESS;
+}
+
+static int check_list(const unsigned* qs, unsigned num, unsigned bound, const char* what, bool allowEmpty) {
+    if (num == 0) return allowEmpty ? DFS_SUCCESS : fail(DFS_ERR_INVALID_ARG, "no %s given", what);
+    if (!qs) return fail(DFS_ERR_INVALID_ARG, "null %s array", what);
+    if (num > (unsigned)kMaxList) return fail(DFS_ERR_TOO_LARGE, "too many %s (%u)", what, num);
+    uint64_t seen = 0;
+    for (unsigned i = 0; i < num; i++) {
+        int rc = check_qubit(qs[i], bound, what);
+        if (rc) return rc;
+        if (seen & (1ull << qs[i])) return fail(DFS_ERR_DUPLICATE_QUBIT, "repeated %s %u", what, qs[i]);
+        seen |= 1ull << qs[i];
+    }
+    return DFS_SUCCESS;
+}
+
+static int check_paulis(const unsigned* p, unsigned num) {
+    if (num && !p) return fail(DFS_ERR_INVALID_ARG, "null pauli array");
+    for (unsigned i = 0; i < num; i++)
+        if (p[i] > 3) return fail(DFS_ERR_INVALID_ARG, "pauli code %u is not in 0..3", p[i]);
+    return DFS_SUCCESS;
+}
+
+static int new_state(unsigned n, int isDM, int precision, dfs_state* out) {
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (!out) return fail(DFS_ERR_INVALID_ARG, "null output handle");
+    if (precision != DFS_C128 && precision != DFS_C128_NATIVE && precision != DFS_C64)
+        return fail(DFS_ERR_PRECISION, "unknown precision %d", precision);
+    unsigned vq = isDM ? 2 * n : n;
+    if (vq > (unsigned)kMaxQubits) return fail(DFS_ERR_TOO_LARGE, "%u qubits exceed the engine limit", n);
+    dfs_state s = new (std::nothrow) dfs_state_s();
+    if (!s) return fail(DFS_ERR_OUT_OF_MEMORY, "host allocation");
+    s->isDM = isDM;
+    s->numQubits = n;
+    s->vecQubits = vq;
+    s->numAmps = 1ull << vq;
+    s->precision = precision;
+    s->amps = nullptr;
+    size_t bytes = s->numAmps * elem_bytes(precision);
+    cudaError_t e = cudaMalloc(&s->amps, bytes);
+    if (e != cudaSuccess) {
+        delete s;
+        return cuda_fail(e, "state allocation");
+    }
+    e = cudaMemsetAsync(s->amps, 0, bytes, g_ctx.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g_ctx.stream);
+    if (e != cudaSuccess) {
+        cudaFree(s->amps);
+        delete s;
+        return cuda_fail(e, "state zero-fill");
+    }
+    *out = s;
+    return DFS_SUCCESS;
+}
+
+static std::vector<unsigned> shifted(const unsigned* t, unsigned k, unsigned by) {
+    std::vector<unsigned> v(t, t + k);
+    for (unsigned& x : v) x += by;
+    return v;
+}
+
+static bool odd_num_y(const unsigned* p, unsigned k) {
+    int c = 0;
+    for (unsigned i = 0; i < k; i++) c += p[i] == 2;
+    return c & 1;
+}
+
+}  // namespace dfs
+
+using namespace dfs;
+
+extern "C" {
+
+const char* dfs_error_string(int code) {
+    switch (code) {
+        case DFS_SUCCESS: return "success";
+        case DFS_ERR_INVALID_ARG: return "invalid argument";
+        case DFS_ERR_QUBIT_INDEX: return "qubit index out of range";
+        case DFS_ERR_DUPLICATE_QUBIT: return "duplicate qubit";
+        case DFS_ERR_STATE_KIND: return "wrong state kind";
+        case DFS_ERR_TOO_LARGE: return "too large";
+        case DFS_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case DFS_ERR_CUDA: return "CUDA error";
+        case DFS_ERR_NOT_INITIALISED: return "not initialised";
+        case DFS_ERR_PRECISION: return "precision mismatch";
+        case DFS_ERR_TIMEOUT: return "device wait timed out";
+        default: return "unknown error";
+    }
+}
+
+const char* dfs_last_error(void) { return g_lastError; }
+
+// ---------------------------------------------------------- environment
+
+int dfs_comm_init(void) { return ensure_init(); }
+
+int dfs_comm_end(void) {
+    if (!g_ctx.initialised) return DFS_SUCCESS;
+    cudaStreamSynchronize(g_ctx.stream);
+    return DFS_SUCCESS;
+}
+
+int dfs_comm_get_rank(unsigned* rank) {
+    if (!rank) return fail(DFS_ERR_INVALID_ARG, "null output");
+    *rank = 0;
+    return DFS_SUCCESS;
+}
+
+int dfs_comm_get_num_nodes(unsigned* n) {
+    if (!n) return fail(DFS_ERR_INVALID_ARG, "null output");
+    *n = 1;
+    return DFS_SUCCESS;
+}
+
+int dfs_comm_synch(void) {
+    int rc = ensure_init();
+    if (rc) return rc;
+    cudaError_t e = cudaStreamSynchronize(g_ctx.stream);
+    return e == cudaSuccess ? DFS_SUCCESS : cuda_fail(e, "comm_synch");
+}
+
+int dfs_set_stream(void* stream) {
+    int rc = ensure_init();
+    if (rc) return rc;
+    g_ctx.stream = stream ? (cudaStream_t)stream : g_ctx.ownStream;
+    return DFS_SUCCESS;
+}
+
+int dfs_get_stream(void** stream) {
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (!stream) return fail(DFS_ERR_INVALID_ARG, "null output");
+    *stream = (void*)g_ctx.stream;
+    return DFS_SUCCESS;
+}
+
+// ---------------------------------------------------------------- states
+
+int dfs_statevector_create(unsigned n, int precision, dfs_state* out) { return new_state(n, 0, precision, out); }
+int dfs_densitymatrix_create(unsigned n, int precision, dfs_state* out) { return new_state(n, 1, precision, out); }
+
+int dfs_state_destroy(dfs_state s) {
+    if (!s) return DFS_SUCCESS;
+    if (g_ctx.initialised) cudaStreamSynchronize(g_ctx.stream);
+    cudaFree(s->amps);
+    delete s;
+    return DFS_SUCCESS;
+}
+
+int dfs_state_get_info(dfs_state s, dfs_state_info* info) {
+    if (!s || !info) return fail(DFS_ERR_INVALID_ARG, "null argument");
+    info->rank = 0;
+    info->num_nodes = 1;
+    info->log_num_nodes = 0;
+    info->num_qubits = s->numQubits;
+    info->num_amps_per_node = s->numAmps;
+    info->log_num_amps_per_node = s->vecQubits;
+    info->is_density_matrix = s->isDM;
+    info->precision = s->precision;
+    return DFS_SUCCESS;
+}
+
+int dfs_state_device_ptr(dfs_state s, void** ptr) {
+    if (!s || !ptr) return fail(DFS_ERR_INVALID_ARG, "null argument");
+    *ptr = s->amps;
+    return DFS_SUCCESS;
+}
+
+static int check_range(dfs_state s, const void* p, uint64_t start, uint64_t count) {
+    int rc = check_state(s);
+    if (rc) return rc;
+    if (count && !p) return fail(DFS_ERR_INVALID_ARG, "null buffer");
+    if (start > s->numAmps || count > s->numAmps - start)
+        return fail(DFS_ERR_INVALID_ARG, "range [%llu, +%llu) exceeds %llu amplitudes", (unsigned long long)start,
+                    (unsigned long long)count, (unsigned long long)s->numAmps);
+    return DFS_SUCCESS;
+}
+
+int dfs_state_set_amps(dfs_state s, const double* amps, uint64_t start, uint64_t count) {
+    int rc = check_range(s, amps, start, count);
+    return rc ? rc : (count ? state_upload(s, amps, start, count) : DFS_SUCCESS);
+}
+
+int dfs_state_get_amps(dfs_state s, double* amps, uint64_t start, uint64_t count) {
+    int rc = check_range(s, amps, start, count);
+    return rc ? rc : (count ? state_download(s, amps, start, count) : DFS_SUCCESS);
+}
+
+int dfs_state_set_raw(dfs_state s, const void* src, uint64_t start, uint64_t count) {
+    int rc = check_range(s, src, start, count);
+    if (rc || !count) return rc;
+    size_t eb = elem_bytes(s->precision);
+    cudaError_t e =
+        cudaMemcpyAsync((char*)s->amps + start * eb, src, count * eb, cudaMemcpyHostToDevice, g_ctx.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g_ctx.stream);
+    return e == cudaSuccess ? DFS_SUCCESS : cuda_fail(e, "set_raw");
+}
+
+int dfs_state_get_raw(dfs_state s, void* dst, uint64_t start, uint64_t count) {
+    int rc = check_range(s, dst, start, count);
+    if (rc || !count) return rc;
+    size_t eb = elem_bytes(s->precision);
+    cudaError_t e =
+        cudaMemcpyAsync(dst, (const char*)s->amps + start * eb, count * eb, cudaMemcpyDeviceToHost, g_ctx.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g_ctx.stream);
+    return e == cudaSuccess ? DFS_SUCCESS : cuda_fail(e, "get_raw");
+}
+
+int dfs_state_copy(dfs_state dst, dfs_state src) {
+    int rc = check_state(dst);
+    if (!rc) rc = check_state(src);
+    if (rc) return rc;
+    if (dst->numAmps != src->numAmps || dst->isDM != src->isDM || dst->numQubits != src->numQubits)
+        return fail(DFS_ERR_INVALID_ARG, "states differ in shape");
+    if (elem_bytes(dst->precision) != elem_bytes(src->precision))
+        return fail(DFS_ERR_PRECISION, "states differ in precision");
+    if (dst == src) return DFS_SUCCESS;
+    cudaError_t e = cudaMemcpyAsync(dst->amps, src->amps, src->numAmps * elem_bytes(src->precision),
+                                    cudaMemcpyDeviceToDevice, g_ctx.stream);
+    return e == cudaSuccess ? DFS_SUCCESS : cuda_fail(e, "state copy");
+}
+
+int dfs_state_set_zero(dfs_state s) {
+    int rc = check_state(s);
+    return rc ? rc : state_fill_zero(s);
+}
+
+int dfs_state_set_classical(dfs_state s, uint64_t index) {
+    int rc = check_state(s);
+    if (rc) return rc;
+    if (index >= s->numAmps) return fail(DFS_ERR_INVALID_ARG, "index %llu out of range", (unsigned long long)index);
+    return state_set_classical(s, index);
+}
+
+int dfs_state_set_random(dfs_state s, uint64_t seed, int normalise) {
+    int rc = check_state(s);
+    return rc ? rc : state_set_random(s, seed, normalise);
+}
+
+// ------------------------------------------------------ statevector gates
+
+int dfs_statevector_oneTargGate(dfs_state s, unsigned target, const double* gate) {
+    int rc = check_state(s);
+    if (!rc) rc = check_qubit(target, s->vecQubits, "target");
+    if (!rc && !gate) rc = fail(DFS_ERR_INVALID_ARG, "null gate");
+    return rc ? rc : sv_one_targ(s, target, gate);
+}
+
+int dfs_statevector_manyCtrlOneTargGate(dfs_state s, const unsigned* controls, unsigned nc, unsigned target,
+                                        const double* gate) {
+    int rc = check_state(s);
+    if (!rc) rc = check_qubit(target, s->vecQubits, "target");
+    if (!rc) rc = check_list(controls, nc, s->vecQubits, "control", true);
+    if (!rc)
+        for (unsigned i = 0; i < nc; i++)
+            if (controls[i] == target) rc = fail(DFS_ERR_DUPLICATE_QUBIT, "control %u is also the target", target);
+    if (!rc && nc + 1 > s->vecQubits) rc = fail(DFS_ERR_TOO_LARGE, "too many controls");
+    if (!rc && !gate) rc = fail(DFS_ERR_INVALID_ARG, "null gate");
+    return rc ? rc : sv_ctrl_one_targ(s, controls, nc, target, gate);
+}
+
+int dfs_statevector_swapGate(dfs_state s, unsigned qb1, unsigned qb2) {
+    int rc = check_state(s);
+    if (!rc) rc = check_qubit(qb1, s->vecQubits, "qubit");
+    if (!rc) rc = check_qubit(qb2, s->vecQubits, "qubit");
+    if (rc) return rc;
+    return qb1 == qb2 ? DFS_SUCCESS : sv_swap(s, qb1, qb2);
+}
+
+int dfs_statevector_manyTargGate(dfs_state s, const unsigned* targets, unsigned k, const double* gate) {
+    int rc = check_state(s);
+    if (!rc) rc = check_list(targets, k, s->vecQubits, "target", false);
+    if (!rc && !gate) rc = fail(DFS_ERR_INVALID_ARG, "null gate");
+    return rc ? rc : sv_many_targ(s, targets, k, gate);
+}
+
+int dfs_statevector_pauliTensor(dfs_state s, const unsigned* targets, const unsigned* paulis, unsigned k) {
+    int rc = check_state(s);
+    if (!rc) rc = check_list(targets, k, s->vecQubits, "target", true);
+    if (!rc) rc = check_paulis(paulis, k);
+    return rc ? rc : sv_pauli(s, targets, paulis, k, 0, 0.0);
+}
+
+int dfs_statevector_pauliGadget(dfs_state s, const unsigned* targets, const unsigned* paulis, unsigned k,
+                                double theta) {
+    int rc = check_state(s);
+    if (!rc) rc = check_list(targets, k, s->vecQubits, "target", true);
+    if (!rc) rc = check_paulis(paulis, k);
+    return rc ? rc : sv_pauli(s, targets, paulis, k, 1, theta);
+}
+
+int dfs_statevector_phaseGadget(dfs_state s, const unsigned* targets, unsigned k, double theta) {
+    int rc = check_state(s);
+    if (!rc) rc = check_list(targets, k, s->vecQubits, "target", true);
+    return rc ? rc : sv_phase_gadget(s, targets, k, theta);
+}
+
+// --------------------------------------------------------- density matrix
+
+int dfs_densitymatrix_manyTargGate(dfs_state s, const unsigned* targets, unsigned k, const double* gate) {
+    int rc = check_dm(s);
+    if (!rc) rc = check_list(targets, k, s->numQubits, "target", false);
+    if (!rc && !gate) rc = fail(DFS_ERR_INVALID_ARG, "null gate");
+    if (rc) return rc;
+    if ((rc = sv_many_targ(s, targets, k, gate))) return rc;
+    size_t d = (size_t)1 << k;
+    std::vector<double> conjGate(gate, gate + 2 * d * d);
+    for (size_t e = 0; e < d * d; e++) conjGate[2 * e + 1] = -conjGate[2 * e + 1];
+    std::vector<unsigned> bra = shifted(targets, k, s->numQubits);
+    return sv_many_targ(s, bra.data(), k, conjGate.data());
+}
+
+int dfs_densitymatrix_swapGate(dfs_state s, unsigned qb1, unsigned qb2) {
+    int rc = check_dm(s);
+    if (!rc) rc = check_qubit(qb1, s->numQubits, "qubit");
+    if (!rc) rc = check_qubit(qb2, s->numQubits, "qubit");
+    if (rc || qb1 == qb2) return rc;
+    if ((rc = sv_swap(s, qb1, qb2))) return rc;
+    return sv_swap(s, qb1 + s->numQubits, qb2 + s->numQubits);
+}
+
+int dfs_densitymatrix_pauliTensor(dfs_state s, const unsigned* targets, const unsigned* paulis, unsigned k) {
+    int rc = check_dm(s);
+    if (!rc) rc = check_list(targets, k, s->numQubits, "target", true);
+    if (!rc) rc = check_paulis(paulis, k);
+    if (rc) return rc;
+    if ((rc = sv_pauli(s, targets, paulis, k, 0, 0.0))) return rc;
+    std::vector<unsigned> bra = shifted(targets, k, s->numQubits);
+    if ((rc = sv_pauli(s, bra.data(), paulis, k, 0, 0.0))) return rc;
+    return odd_num_y(paulis, k) ? state_scale_real(s, -1.0) : DFS_SUCCESS;
+}
+
+int dfs_densitymatrix_pauliGadget(dfs_state s, const unsigned* targets, const unsigned* paulis, unsigned k,
+                                  double theta) {
+    int rc = check_dm(s);
+    if (!rc) rc = check_list(targets, k, s->numQubits, "target", true);
+    if (!rc) rc = check_paulis(paulis, k);
+    if (rc) return rc;
+    if ((rc = sv_pauli(s, targets, paulis, k, 1, theta))) return rc;
+    std::vector<unsigned> bra = shifted(targets, k, s->numQubits);
+    return sv_pauli(s, bra.data(), paulis, k, 1, odd_num_y(paulis, k) ? theta : -theta);
+}
+
+int dfs_densitymatrix_phaseGadget(dfs_state s, const unsigned* targets, unsigned k, double theta) {
+    int rc = check_dm(s);
+    if (!rc) rc = check_list(targets, k, s->numQubits, "target", true);
+    if (rc) return rc;
+    if ((rc = sv_phase_gadget(s, targets, k, theta))) return rc;
+    std::vector<unsigned> bra = shifted(targets, k, s->numQubits);
+    return sv_phase_gadget(s, bra.data(), k, -theta);
+}
+
+int dfs_densitymatrix_krausMap(dfs_state s, const double* ops, unsigned numOps, const unsigned* targets,
+                               unsigned k) {
+    int rc = check_dm(s);
+    if (!rc) rc = check_list(targets, k, s->numQubits, "target", false);
+    if (!rc && (!ops || numOps == 0)) rc = fail(DFS_ERR_INVALID_ARG, "no Kraus operators given");
+    if (rc) return rc;
+    // getSuperoperator, src/misc.hpp:58-81: S[i*d+k][j*d+l] = sum conj(K[i][j]) K[k][l]
+    const size_t d = (size_t)1 << k, sd = d * d;
+    std::vector<std::complex<double>> S(sd * sd);
+    const std::complex<double>* K = reinterpret_cast<const std::complex<double>*>(ops);
+    for (unsigned o = 0; o < numOps; o++) {
+        const std::complex<double>* M = K + (size_t)o * d * d;
+        for (size_t i = 0; i < d; i++)
+            for (size_t j = 0; j < d; j++) {
+                std::complex<double> cij = std::conj(M[i * d + j]);
+                for (size_t kk = 0; kk < d; kk++)
+                    for (size_t l = 0; l < d; l++) S[(i * d + kk) * sd + (j * d + l)] += cij * M[kk * d + l];
+            }
+    }
+    std::vector<unsigned> ext(targets, targets + k);
+    for (unsigned i = 0; i < k; i++) ext.push_back(targets[i] + s->numQubits);
+    return sv_many_targ(s, ext.data(), 2 * k, reinterpret_cast<const double*>(S.data()));
+}
+
+int dfs_densitymatrix_oneQubitDephasing(dfs_state s, unsigned qb, double prob) {
+    int rc = check_dm(s);
+    if (!rc) rc = check_qubit(qb, s->numQubits, "qubit");
+    return rc ? rc : dm_deph1(s, qb, prob);
+}
+
+static int check_two(dfs_state s, unsigned q1, unsigned q2) {
+    int rc = check_dm(s);
+    if (!rc) rc = check_qubit(q1, s->numQubits, "qubit");
+    if (!rc) rc = check_qubit(q2, s->numQubits, "qubit");
+    if (!rc && q1 == q2) rc = fail(DFS_ERR_DUPLICATE_QUBIT, "the two qubits must differ (both %u)", q1);
+    return rc;
+}
+
+int dfs_densitymatrix_twoQubitDephasing(dfs_state s, unsigned qb1, unsigned qb2, double prob) {
+    int rc = check_two(s, qb1, qb2);
+    return rc ? rc : dm_deph2(s, qb1, qb2, prob);
+}
+
+int dfs_densitymatrix_oneQubitDepolarising(dfs_state s, unsigned qb, double prob) {
+    int rc = check_dm(s);
+    if (!rc) rc = check_qubit(qb, s->numQubits, "qubit");
+    return rc ? rc : dm_depol1(s, qb, prob);
+}
+
+int dfs_densitymatrix_twoQubitDepolarising(dfs_state s, unsigned qb1, unsigned qb2, double prob) {
+    int rc = check_two(s, qb1, qb2);
+    return rc ? rc : dm_depol2(s, qb1, qb2, prob, 0);
+}
+
+int dfs_densitymatrix_twoQubitDepolarising_referenceCompat(dfs_state s, unsigned qb1, unsigned qb2, double prob) {
+    int rc = check_two(s, qb1, qb2);
+    return rc ? rc : dm_depol2(s, qb1, qb2, prob, 1);
+}
+
+int dfs_densitymatrix_damping(dfs_state s, unsigned qb, double prob) {
+    int rc = check_dm(s);
+    if (!rc) rc = check_qubit(qb, s->numQubits, "qubit");
+    return rc ? rc : dm_damping(s, qb, prob);
+}
+
+int dfs_densitymatrix_expecPauliString(dfs_state s, const double* coeffs, unsigned numTerms,
+                                       const unsigned* allPaulis, double* re, double* im) {
+    int rc = check_dm(s);
+    if (!rc && (!re || !im)) rc = fail(DFS_ERR_INVALID_ARG, "null output");
+    if (!rc && numTerms && (!coeffs || !allPaulis)) rc = fail(DFS_ERR_INVALID_ARG, "null term arrays");
+    if (!rc) rc = check_paulis(allPaulis, numTerms * s->numQubits);
+    if (rc) return rc;
+    if (numTerms == 0) {
+        *re = 0;
+        *im = 0;
+        return DFS_SUCCESS;
+    }
+    return dm_expec_pauli(s, coeffs, numTerms, allPaulis, re, im);
+}
+
+int dfs_densitymatrix_partialTrace(dfs_state s, const unsigned* targets, unsigned k, dfs_state* out) {
+    int rc = check_dm(s);
+    if (!rc) rc = check_list(targets, k, s->numQubits, "target", true);
+    if (!rc && !out) rc = fail(DFS_ERR_INVALID_ARG, "null output handle");
+    if (rc) return rc;
+    dfs_state r = nullptr;
+    if ((rc = new_state(s->numQubits - k, 1, s->precision, &r))) return rc;
+    if ((rc = dm_partial_trace(s, targets, k, r))) {
+        dfs_state_destroy(r);
+        return rc;
+    }
+    *out = r;
+    return DFS_SUCCESS;
+}
+
+// --------------------------------------------------------------- additions
+
+int dfs_statevector_expecPauliSum(dfs_state s, const double* coeffs, unsigned numTerms, const unsigned* allPaulis,
+                                  double* re, double* im) {
+    int rc = check_state(s);
+    if (!rc && (!re || !im)) rc = fail(DFS_ERR_INVALID_ARG, "null output");
+    if (!rc && numTerms && (!coeffs || !allPaulis)) rc = fail(DFS_ERR_INVALID_ARG, "null term arrays");
+    if (!rc) rc = check_paulis(allPaulis, numTerms * s->vecQubits);
+    if (rc) return rc;
+    if (numTerms == 0) {
+        *re = 0;
+        *im = 0;
+        return DFS_SUCCESS;
+    }
+    State view = *s;
+    view.numQubits = s->vecQubits;  // terms address every bit of the vector
+    return sv_expec_pauli_sum(&view, coeffs, numTerms, allPaulis, re, im);
+}
+
+int dfs_state_inner_product(dfs_state a, dfs_state b, double* re, double* im) {
+    int rc = check_state(a);
+    if (!rc) rc = check_state(b);
+    if (!rc && (!re || !im)) rc = fail(DFS_ERR_INVALID_ARG, "null output");
+    if (rc) return rc;
+    if (a->numAmps != b->numAmps) return fail(DFS_ERR_INVALID_ARG, "states differ in size");
+    if (a->precision != b->precision) return fail(DFS_ERR_PRECISION, "states differ in precision");
+    return state_inner(a, b, re, im);
+}
+
+int dfs_state_norm_squared(dfs_state s, double* out) {
+    int rc = check_state(s);
+    if (!rc && !out) rc = fail(DFS_ERR_INVALID_ARG, "null output");
+    return rc ? rc : state_norm2(s, out);
+}
+
+int dfs_densitymatrix_trace(dfs_state s, double* re, double* im) {
+    int rc = check_dm(s);
+    if (!rc && (!re || !im)) rc = fail(DFS_ERR_INVALID_ARG, "null output");
+    return rc ? rc : dm_trace(s, re, im);
+}
+
+}  // extern "C"

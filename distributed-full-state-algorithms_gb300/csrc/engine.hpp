@@ -1,0 +1,90 @@
+// engine.hpp -- host-side internals shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "../../include/dfs_gb300.h"
+#include "common.cuh"
+
+namespace dfs {
+
+struct Context {
+    bool initialised = false;
+    int device = 0;
+    int numSMs = kNumSMs;
+    size_t smemOptin = 48 * 1024;
+    cudaStream_t ownStream = nullptr;
+    cudaStream_t stream = nullptr;
+    // device scratch for per-call tables (gate matrices, reduction partials);
+    // reused across calls in stream order, grown on demand
+    void* scratch = nullptr;
+    size_t scratchBytes = 0;
+    // pinned host staging for small uploads that must outlive the call
+    void* pinned = nullptr;
+    size_t pinnedBytes = 0;
+    cudaEvent_t pinnedFree = nullptr;
+};
+
+Context& ctx();
+
+struct State {
+    int isDM;
+    unsigned numQubits;   // n (of the matrix for a density matrix)
+    unsigned vecQubits;   // n, or 2n for a density matrix
+    uint64_t numAmps;     // 2^vecQubits
+    int precision;
+    void* amps;
+};
+
+// records a message for dfs_last_error and returns code
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t err, const char* what);
+
+// device scratch of at least `bytes`; returns nullptr on failure (error recorded)
+void* scratch(size_t bytes);
+// copy `bytes` from host to a fresh region of device scratch at byte offset
+// `offset` through pinned staging, ordered on the context stream
+int upload_scratch(const void* host, size_t bytes, size_t offset);
+
+inline size_t elem_bytes(int precision) { return precision == DFS_C64 ? 8 : 16; }
+
+// ---- launchers implemented in the kernel translation units ----
+// All take validated arguments.  Gate matrices are row-major interleaved doubles.
+
+// k_sv.cu
+int sv_one_targ(State* s, unsigned t, const double* gate);
+int sv_ctrl_one_targ(State* s, const unsigned* ctrls, unsigned nc, unsigned t, const double* gate);
+int sv_swap(State* s, unsigned q1, unsigned q2);
+int sv_many_targ(State* s, const unsigned* targs, unsigned k, const double* gate);
+int sv_pauli(State* s, const unsigned* targs, const unsigned* paulis, unsigned k, int gadget, double theta);
+int sv_phase_gadget(State* s, const unsigned* targs, unsigned k, double theta);
+int state_scale_real(State* s, double factor);
+
+// k_dm.cu
+int dm_deph1(State* s, unsigned q, double p);
+int dm_deph2(State* s, unsigned q1, unsigned q2, double p);
+int dm_depol1(State* s, unsigned q, double p);
+int dm_depol2(State* s, unsigned q1, unsigned q2, double p, int referenceCompat);
+int dm_damping(State* s, unsigned q, double p);
+int dm_expec_pauli(State* s, const double* coeffs, unsigned numTerms, const unsigned* allPaulis, double* re,
+                   double* im);
+int dm_partial_trace(State* in, const unsigned* targs, unsigned k, State* out);
+
+// k_util.cu
+int state_fill_zero(State* s);
+int state_set_classical(State* s, uint64_t index);
+int state_set_random(State* s, uint64_t seed, int normalise);
+int state_upload(State* s, const double* amps, uint64_t start, uint64_t count);
+int state_download(State* s, double* amps, uint64_t start, uint64_t count);
+int sv_expec_pauli_sum(State* s, const double* coeffs, unsigned numTerms, const unsigned* allPaulis, double* re,
+                       double* im);
+int state_inner(State* a, State* b, double* re, double* im);
+int state_norm2(State* s, double* out);
+int dm_trace(State* s, double* re, double* im);
+
+}  // namespace dfs
+
+struct dfs_state_s : dfs::State {};

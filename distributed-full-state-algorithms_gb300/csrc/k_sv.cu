@@ -1,0 +1,424 @@
+// k_sv.cu -- statevector amplitude kernels (rows a3-a8 of the engine's scope):
+// the loops of the reference's src/local_statevector.hpp as sm_103a kernels.
+//
+// Every kernel streams the state once, in place.  Work items are amplitude
+// pairs, groups or single amplitudes addressed by per-thread bit deposit
+// (common.cuh); each thread keeps two items in flight so that a warp has four
+// independent 16-byte loads outstanding, and grid-stride loops size the grid
+// to the SM count.  Arithmetic goes through the state's policy (common.cuh).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "kernels.cuh"
+
+namespace dfs {
+
+// ------------------------------------------------------------ one target
+// local_statevector_oneTargGate, src/local_statevector.hpp:14-29
+
+template <class P, class IT>
+struct OneTargOp {
+    typename P::K g[4];
+    int t;
+    DEV void index(IT j, IT& i0, IT& i1) const {
+        i0 = insert_zero(j, t);
+        i1 = i0 | ((IT)1 << t);
+    }
+    DEV void apply(IT, IT, typename P::V& x0, typename P::V& x1) const {
+        typename P::A a0 = P::first(g[0], x0);
+        P::mac(a0, g[1], x1);
+        typename P::A a1 = P::first(g[2], x0);
+        P::mac(a1, g[3], x1);
+        x0 = P::get(a0);
+        x1 = P::get(a1);
+    }
+};
+
+struct RunOneTarg {
+    template <class P, class IT>
+    static int run(State* s, unsigned t, const double* g) {
+        OneTargOp<P, IT> op;
+        op.t = (int)t;
+        for (int i = 0; i < 4; i++) op.g[i] = P::mk(g[2 * i], g[2 * i + 1]);
+        IT items = (IT)(s->numAmps / 2);
+        return launch(k_pair<P, IT, OneTargOp<P, IT>>, items, kPer, "oneTargGate", (typename P::store*)s->amps,
+                      items, op);
+    }
+};
+int sv_one_targ(State* s, unsigned t, const double* gate) { return dispatch<RunOneTarg>(s, s, t, gate); }
+
+// ------------------------------------------------ many controls, one target
+// local_statevector_manyCtrlOneTargGate, src/local_statevector.hpp:32-51
+
+template <class P, class IT>
+struct CtrlOneTargOp {
+    typename P::K g[4];
+    QList q;        // controls and target, sorted
+    IT setMask;     // all control bits and the target bit
+    IT tbit;
+    DEV void index(IT j, IT& i0, IT& i1) const {
+        i1 = insert_zeros(j, q) | setMask;
+        i0 = i1 ^ tbit;
+    }
+    DEV void apply(IT, IT, typename P::V& x0, typename P::V& x1) const {
+        typename P::A a0 = P::first(g[0], x0);
+        P::mac(a0, g[1], x1);
+        typename P::A a1 = P::first(g[2], x0);
+        P::mac(a1, g[3], x1);
+        x0 = P::get(a0);
+        x1 = P::get(a1);
+    }
+};
+
+struct RunCtrlOneTarg {
+    template <class P, class IT>
+    static int run(State* s, const unsigned* ctrls, unsigned nc, unsigned t, const double* g) {
+        CtrlOneTargOp<P, IT> op;
+        std::vector<unsigned> qs(ctrls, ctrls + nc);
+        qs.push_back(t);
+        op.q = make_qlist(qs);
+        uint64_t m = 0;
+        for (unsigned q : qs) m |= 1ull << q;
+        op.setMask = (IT)m;
+        op.tbit = (IT)(1ull << t);
+        for (int i = 0; i < 4; i++) op.g[i] = P::mk(g[2 * i], g[2 * i + 1]);
+        IT items = (IT)(s->numAmps >> (nc + 1));
+        return launch(k_pair<P, IT, CtrlOneTargOp<P, IT>>, items, kPer, "manyCtrlOneTargGate",
+                      (typename P::store*)s->amps, items, op);
+    }
+};
+int sv_ctrl_one_targ(State* s, const unsigned* ctrls, unsigned nc, unsigned t, const double* gate) {
+    return dispatch<RunCtrlOneTarg>(s, s, ctrls, nc, t, gate);
+}
+
+// ------------------------------------------------------------------- swap
+// local_statevector_swapGate, src/local_statevector.hpp:54-69: exchange the
+// amplitudes whose (qb2, qb1) bits are 01 and 10; pure data movement.
+
+template <class IT>
+struct SwapOp {
+    int lo, hi;  // lo < hi
+    DEV void index(IT k, IT& i0, IT& i1) const {
+        IT b = insert_zero(insert_zero(k, lo), hi);
+        i0 = b | ((IT)1 << lo);
+        i1 = b | ((IT)1 << hi);
+    }
+    template <class S>
+    DEV void apply_raw(IT, IT, S& x0, S& x1) const {
+        S t = x0;
+        x0 = x1;
+        x1 = t;
+    }
+};
+
+struct RunSwap {
+    template <class P, class IT>
+    static int run(State* s, unsigned q1, unsigned q2) {
+        SwapOp<IT> op{(int)std::min(q1, q2), (int)std::max(q1, q2)};
+        IT items = (IT)(s->numAmps / 4);
+        using S = typename P::store;
+        return launch(k_pair_raw<S, IT, SwapOp<IT>>, items, kPer, "swapGate", (S*)s->amps, items, op);
+    }
+};
+int sv_swap(State* s, unsigned q1, unsigned q2) { return dispatch<RunSwap>(s, s, q1, q2); }
+
+// --------------------------------------------------------- Pauli strings
+// distributed_statevector_pauliTensorOrGadget, src/distributed_statevector.hpp:244-276, and
+// local_statevector_pauliTensorOrGadget_subroutine, src/local_statevector.hpp:102-135:
+//   (P psi)[j] = i^{#Y} (-1)^{parity((j ^ X) & YZ)} psi[j ^ X]
+// Tensor: psi <- P psi.  Gadget: psi <- cos(theta) psi + i sin(theta) P psi.
+
+template <class P, class IT>
+struct PauliGadgetOp {
+    typename P::R c, sn;
+    IT maskX, maskYZ;
+    int top;   // highest X/Y qubit: pairs (j, j ^ X) with this bit 0
+    int powY;  // #Y mod 4, plus one for the factor i of the gadget
+    DEV void index(IT j, IT& i0, IT& i1) const {
+        i0 = insert_zero(j, top);
+        i1 = i0 ^ maskX;
+    }
+    DEV void apply(IT i0, IT i1, typename P::V& x0, typename P::V& x1) const {
+        int s0 = parity(i0 & maskYZ), s1 = parity(i1 & maskYZ);
+        typename P::A a0 = P::first_r(c, x0);
+        P::mac_r(a0, sn, rot<P>(x1, powY, s1));
+        typename P::A a1 = P::first_r(c, x1);
+        P::mac_r(a1, sn, rot<P>(x0, powY, s0));
+        x0 = P::get(a0);
+        x1 = P::get(a1);
+    }
+};
+
+template <class IT>
+struct PauliTensorOp {
+    IT maskX, maskYZ;
+    int top, powY;
+    DEV void index(IT j, IT& i0, IT& i1) const {
+        i0 = insert_zero(j, top);
+        i1 = i0 ^ maskX;
+    }
+    template <class S>
+    DEV void apply_raw(IT i0, IT i1, S& x0, S& x1) const {
+        int s0 = parity(i0 & maskYZ), s1 = parity(i1 & maskYZ);
+        S y0 = raw_rot(x1, powY, s1);
+        S y1 = raw_rot(x0, powY, s0);
+        x0 = y0;
+        x1 = y1;
+    }
+};
+
+// strings without X or Y are diagonal: (P psi)[j] = (-1)^{parity(j & Z)} psi[j]
+// (the reference loop runs zero times for them; this applies the maths)
+template <class P, class IT>
+struct DiagPhaseOp {   // x * (parity ? k1 : k0)
+    typename P::K k0, k1;
+    IT mask;
+    DEV typename P::V apply(IT j, typename P::V x) const { return P::mul(parity(j & mask) ? k1 : k0, x); }
+};
+
+template <class IT>
+struct DiagSignOp {
+    IT mask;
+    template <class S>
+    DEV S apply_raw(IT j, S x) const { return parity(j & mask) ? raw_neg(x) : x; }
+};
+
+struct RunPauli {
+    template <class P, class IT>
+    static int run(State* s, const unsigned* targs, const unsigned* paulis, unsigned k, int gadget, double theta) {
+        uint64_t mX = 0, mYZ = 0;
+        int numY = 0, top = -1;
+        for (unsigned i = 0; i < k; i++) {
+            if (paulis[i] == 1 || paulis[i] == 2) {
+                mX |= 1ull << targs[i];
+                top = std::max(top, (int)targs[i]);
+            }
+            if (paulis[i] == 2 || paulis[i] == 3) mYZ ^= 1ull << targs[i];
+            if (paulis[i] == 2) numY++;
+        }
+        using S = typename P::store;
+        if (mX == 0) {
+            IT items = (IT)s->numAmps;
+            if (!gadget) {
+                if (mYZ == 0) return DFS_SUCCESS;  // identity
+                DiagSignOp<IT> op{(IT)mYZ};
+                return launch(k_diag_raw<S, IT, DiagSignOp<IT>>, items, 4, "pauliTensor", (S*)s->amps, items, op);
+            }
+            // exp(i theta Z..Z): e^{+i theta} on even parity, e^{-i theta} on odd
+            DiagPhaseOp<P, IT> op;
+            op.k0 = P::mk(std::cos(theta), std::sin(theta));
+            op.k1 = P::mk(std::cos(theta), -std::sin(theta));
+            op.mask = (IT)mYZ;
+            return launch(k_diag<P, IT, DiagPhaseOp<P, IT>>, items, 4, "pauliGadget", (typename P::store*)s->amps,
+                          items, op);
+        }
+        IT items = (IT)(s->numAmps / 2);
+        if (!gadget) {
+            PauliTensorOp<IT> op{(IT)mX, (IT)mYZ, top, numY & 3};
+            return launch(k_pair_raw<S, IT, PauliTensorOp<IT>>, items, kPer, "pauliTensor", (S*)s->amps, items, op);
+        }
+        PauliGadgetOp<P, IT> op;
+        op.c = P::mkr(std::cos(theta));
+        op.sn = P::mkr(std::sin(theta));
+        op.maskX = (IT)mX;
+        op.maskYZ = (IT)mYZ;
+        op.top = top;
+        op.powY = (numY + 1) & 3;
+        return launch(k_pair<P, IT, PauliGadgetOp<P, IT>>, items, kPer, "pauliGadget", (typename P::store*)s->amps,
+                      items, op);
+    }
+};
+int sv_pauli(State* s, const unsigned* targs, const unsigned* paulis, unsigned k, int gadget, double theta) {
+    return dispatch<RunPauli>(s, s, targs, paulis, k, gadget, theta);
+}
+
+// ------------------------------------------------------------ phase gadget
+// local_statevector_phaseGadget, src/local_statevector.hpp:138-153
+
+struct RunPhaseGadget {
+    template <class P, class IT>
+    static int run(State* s, const unsigned* targs, unsigned k, double theta) {
+        uint64_t m = 0;
+        for (unsigned i = 0; i < k; i++) m ^= 1ull << targs[i];
+        DiagPhaseOp<P, IT> op;
+        op.k0 = P::mk(std::cos(theta), std::sin(theta));
+        op.k1 = P::mk(std::cos(theta), -std::sin(theta));
+        op.mask = (IT)m;
+        IT items = (IT)s->numAmps;
+        return launch(k_diag<P, IT, DiagPhaseOp<P, IT>>, items, 4, "phaseGadget", (typename P::store*)s->amps, items,
+                      op);
+    }
+};
+int sv_phase_gadget(State* s, const unsigned* targs, unsigned k, double theta) {
+    return dispatch<RunPhaseGadget>(s, s, targs, k, theta);
+}
+
+// --------------------------------------------------------- real scaling
+
+template <class IT>
+struct NegateOp {
+    template <class S>
+    DEV S apply_raw(IT, S x) const { return raw_neg(x); }
+};
+
+template <class P, class IT>
+struct ScaleOp {
+    typename P::R c;
+    DEV typename P::V apply(IT, typename P::V x) const { return P::scale(c, x); }
+};
+
+struct RunScale {
+    template <class P, class IT>
+    static int run(State* s, double f) {
+        IT items = (IT)s->numAmps;
+        if (f == -1.0) {
+            using S = typename P::store;
+            return launch(k_diag_raw<S, IT, NegateOp<IT>>, items, 4, "negate", (S*)s->amps, items, NegateOp<IT>{});
+        }
+        ScaleOp<P, IT> op{P::mkr(f)};
+        return launch(k_diag<P, IT, ScaleOp<P, IT>>, items, 4, "scale", (typename P::store*)s->amps, items, op);
+    }
+};
+int state_scale_real(State* s, double factor) { return dispatch<RunScale>(s, s, factor); }
+
+// ------------------------------------------------------------ many targets
+// local_statevector_manyTargGate, src/local_statevector.hpp:72-99: for each
+// group of 2^k amplitudes sharing the non-target bits, out = G in, where bit i
+// of the local index addresses targets[i].
+
+// k <= 3: one group per thread, gate in kernel parameters
+template <class P, class IT, int K>
+struct ManyTargRegOp {
+    QList q;                                 // targets, sorted
+    IT off[1 << K];                          // local index -> amplitude offset
+    typename P::K g[1 << K][1 << K];
+};
+
+template <class P, class IT, int K>
+__global__ void __launch_bounds__(kThreads) k_many_targ_reg(typename P::store* __restrict__ a, IT items,
+                                                            ManyTargRegOp<P, IT, K> op) {
+    constexpr int D = 1 << K;
+    const IT stride = (IT)gridDim.x * kThreads;
+    for (IT j = (IT)blockIdx.x * kThreads + threadIdx.x; j < items; j += stride) {
+        IT b = insert_zeros(j, op.q);
+        typename P::V x[D];
+#pragma unroll
+        for (int c = 0; c < D; c++) x[c] = P::load(a, b + op.off[c]);
+#pragma unroll
+        for (int r = 0; r < D; r++) {
+            typename P::A acc = P::first(op.g[r][0], x[0]);
+#pragma unroll
+            for (int c = 1; c < D; c++) P::mac(acc, op.g[r][c], x[c]);
+            P::save(a, b + op.off[r], P::get(acc));
+        }
+    }
+}
+
+// k >= 4: a CTA stages whole groups in shared memory; one thread per output
+// amplitude reads the gate column-major from device memory (L1/L2 resident).
+constexpr int kMaxSmemTargets = 13;
+
+template <class IT>
+struct GroupShape {
+    QList q;
+    int targets[kMaxSmemTargets];
+    int k;
+};
+
+template <class IT>
+DEV IT group_offset(int local, const GroupShape<IT>& sh) {
+    IT o = 0;
+    for (int b = 0; b < sh.k; b++) o |= (IT)((local >> b) & 1) << sh.targets[b];
+    return o;
+}
+
+template <class P, class IT>
+__global__ void __launch_bounds__(kThreads) k_many_targ_smem(typename P::store* __restrict__ a, IT numGroups,
+                                                             GroupShape<IT> sh, const typename P::K* __restrict__ gT) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    typename P::V* xs = reinterpret_cast<typename P::V*>(smem_raw);
+    const int dim = 1 << sh.k;
+    const int gpc = dim >= kThreads ? 1 : kThreads / dim;  // groups per CTA trip
+    const int span = gpc * dim;
+    for (IT g0 = (IT)blockIdx.x * gpc; g0 < numGroups; g0 += (IT)gridDim.x * gpc) {
+        for (int e = threadIdx.x; e < span; e += kThreads) {
+            IT g = g0 + (IT)(e / dim);
+            if (g < numGroups) xs[e] = P::load(a, insert_zeros(g, sh.q) + group_offset(e % dim, sh));
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < span; e += kThreads) {
+            int gg = e / dim, r = e % dim;
+            IT g = g0 + (IT)gg;
+            if (g < numGroups) {
+                const typename P::V* xg = xs + gg * dim;
+                typename P::A acc = P::first(gT[r], xg[0]);
+                for (int c = 1; c < dim; c++) P::mac(acc, gT[(size_t)c * dim + r], xg[c]);
+                P::save(a, insert_zeros(g, sh.q) + group_offset(r, sh), P::get(acc));
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <class P, class IT, int K>
+static int many_targ_reg(State* s, const unsigned* targs, const double* g) {
+    constexpr int D = 1 << K;
+    ManyTargRegOp<P, IT, K> op;
+    op.q = make_qlist(std::vector<unsigned>(targs, targs + K));
+    for (int c = 0; c < D; c++) {
+        uint64_t o = 0;
+        for (int b = 0; b < K; b++) o |= (uint64_t)((c >> b) & 1) << targs[b];
+        op.off[c] = (IT)o;
+    }
+    for (int r = 0; r < D; r++)
+        for (int c = 0; c < D; c++) op.g[r][c] = P::mk(g[2 * (r * D + c)], g[2 * (r * D + c) + 1]);
+    IT items = (IT)(s->numAmps >> K);
+    return launch(k_many_targ_reg<P, IT, K>, items, 1, "manyTargGate", (typename P::store*)s->amps, items, op);
+}
+
+struct RunManyTarg {
+    template <class P, class IT>
+    static int run(State* s, const unsigned* targs, unsigned k, const double* g) {
+        switch (k) {
+            case 1: return many_targ_reg<P, IT, 1>(s, targs, g);
+            case 2: return many_targ_reg<P, IT, 2>(s, targs, g);
+            case 3: return many_targ_reg<P, IT, 3>(s, targs, g);
+            default: break;
+        }
+        if (k > (unsigned)kMaxSmemTargets)
+            return fail(DFS_ERR_TOO_LARGE, "manyTargGate supports at most %d targets (got %u)", kMaxSmemTargets, k);
+        const size_t dim = (size_t)1 << k;
+        std::vector<typename P::K> gT(dim * dim);
+        for (size_t r = 0; r < dim; r++)
+            for (size_t c = 0; c < dim; c++) gT[c * dim + r] = P::mk(g[2 * (r * dim + c)], g[2 * (r * dim + c) + 1]);
+        int rc = upload_scratch(gT.data(), gT.size() * sizeof(typename P::K), 0);
+        if (rc) return rc;
+        GroupShape<IT> sh;
+        sh.q = make_qlist(std::vector<unsigned>(targs, targs + k));
+        sh.k = (int)k;
+        for (unsigned b = 0; b < k; b++) sh.targets[b] = (int)targs[b];
+        size_t span = dim >= (size_t)kThreads ? dim : (size_t)kThreads;
+        size_t smem = span * sizeof(typename P::V);
+        auto kern = k_many_targ_smem<P, IT>;
+        if (smem > 48 * 1024) {
+            if (smem > ctx().smemOptin)
+                return fail(DFS_ERR_TOO_LARGE, "manyTargGate with %u targets needs %zu B of shared memory", k, smem);
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
+        }
+        IT groups = (IT)(s->numAmps >> k);
+        size_t gpc = dim >= (size_t)kThreads ? 1 : (size_t)kThreads / dim;
+        uint64_t ctas = (groups + gpc - 1) / gpc;
+        uint64_t cap = (uint64_t)ctx().numSMs * 4;
+        unsigned grid = (unsigned)std::max<uint64_t>(1, std::min(ctas, cap));
+        kern<<<grid, kThreads, smem, ctx().stream>>>((typename P::store*)s->amps, groups, sh,
+                                                     (const typename P::K*)ctx().scratch);
+        return check_launch("manyTargGate");
+    }
+};
+int sv_many_targ(State* s, const unsigned* targs, unsigned k, const double* gate) {
+    return dispatch<RunManyTarg>(s, s, targs, k, gate);
+}
+
+}  // namespace dfs

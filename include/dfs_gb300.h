@@ -1,0 +1,203 @@
+/*
+ * dfs_gb300.h -- C ABI of the GB300 full-state engine.
+ *
+ * The engine keeps one quantum state per handle resident in the HBM of one
+ * GPU and applies the operations of TysonRayJones/Distributed-Full-State-
+ * Algorithms to it with hand-written sm_103a kernels.  Each entry point below
+ * replaces one function of that project's header-only C++ API (cited as
+ * file:line of the reference project); the reference's by-value std::vector
+ * arguments become plain pointers plus counts, its assert()s become status
+ * codes, and its single-rank MPI environment becomes a no-op context.
+ *
+ * Conventions (identical to the reference):
+ *  - qubit q is bit q of an amplitude index (qubit 0 least significant);
+ *  - a density matrix of n qubits is a 2n-qubit vector in column-major order,
+ *    amps[c * 2^n + r] = rho[r][c]; its ket qubits are bits 0..n-1, its bra
+ *    qubits bits n..2n-1;
+ *  - a gate on k targets is a row-major 2^k x 2^k complex matrix given as
+ *    interleaved doubles (re, im); bit i of its row/column index addresses
+ *    targets[i] (caller order, not sorted);
+ *  - Pauli codes: 0 = I, 1 = X, 2 = Y, 3 = Z;
+ *  - amplitudes cross the ABI as interleaved doubles (re, im), whatever the
+ *    state's device precision.
+ *
+ * Every function returns DFS_SUCCESS (0) or an error code; dfs_error_string()
+ * names a code and dfs_last_error() describes the latest failure.  Argument
+ * errors are detected on the host before any GPU work is issued.  Work is
+ * ordered on the context's CUDA stream; calls that return host data
+ * (get_amps, reductions) synchronise that stream.
+ */
+#ifndef DFS_GB300_H
+#define DFS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+
+enum {
+    DFS_SUCCESS = 0,
+    DFS_ERR_INVALID_ARG = 1,     /* null pointer, zero count, bad enum */
+    DFS_ERR_QUBIT_INDEX = 2,     /* a qubit index >= the state's qubit count */
+    DFS_ERR_DUPLICATE_QUBIT = 3, /* repeated target / control, or control == target */
+    DFS_ERR_STATE_KIND = 4,      /* statevector passed where a density matrix is required, or vice versa */
+    DFS_ERR_TOO_LARGE = 5,       /* qubit or target count beyond what the engine supports */
+    DFS_ERR_OUT_OF_MEMORY = 6,   /* device allocation failed */
+    DFS_ERR_CUDA = 7,            /* a CUDA runtime call failed */
+    DFS_ERR_NOT_INITIALISED = 8, /* dfs_comm_init() has not been called */
+    DFS_ERR_PRECISION = 9,       /* states of different precisions combined */
+    DFS_ERR_TIMEOUT = 10         /* a bounded device-side wait gave up */
+};
+
+const char* dfs_error_string(int code);
+/* message of the most recent failure on the calling thread ("" if none) */
+const char* dfs_last_error(void);
+
+/* ----------------------------------------------------------- environment */
+/* src/communication.hpp:16-47.  One process drives one GPU: rank 0 of 1. */
+
+int dfs_comm_init(void);                   /* comm_init, src/communication.hpp:16-21 */
+int dfs_comm_end(void);                    /* comm_end, src/communication.hpp:24-27 */
+int dfs_comm_get_rank(unsigned* rank);     /* comm_getRank, src/communication.hpp:30-34 */
+int dfs_comm_get_num_nodes(unsigned* n);   /* comm_getNumNodes, src/communication.hpp:37-41 */
+int dfs_comm_synch(void);                  /* comm_synch, src/communication.hpp:44-47: drains the stream */
+
+/* Work is issued on this CUDA stream (a cudaStream_t; NULL = the engine's own). */
+int dfs_set_stream(void* cuda_stream);
+int dfs_get_stream(void** cuda_stream);
+
+/* ----------------------------------------------------------------- states */
+
+/* device precision of a state */
+enum {
+    DFS_C128 = 0,        /* complex128 storage; FP64-class double-float arithmetic on the FP32 pipes */
+    DFS_C128_NATIVE = 1, /* complex128 storage; native FP64 arithmetic */
+    DFS_C64 = 2          /* complex64 storage and FP32 sweeps; reductions accumulate in double-float */
+};
+
+typedef struct dfs_state_s* dfs_state;
+
+/* StateVector(numQubits), src/states.hpp:32-49.  Amplitudes are zero (not |0>),
+ * as in the reference (src/states.hpp:46-47); there is no exchange buffer. */
+int dfs_statevector_create(unsigned num_qubits, int precision, dfs_state* out);
+/* DensityMatrix(numQubits), src/states.hpp:54-69: a 2n-qubit vector */
+int dfs_densitymatrix_create(unsigned num_qubits, int precision, dfs_state* out);
+int dfs_state_destroy(dfs_state s);
+
+/* the public fields of the reference's state (src/states.hpp:16-23) at one rank */
+typedef struct {
+    unsigned rank;              /* 0 */
+    unsigned num_nodes;         /* 1 */
+    unsigned log_num_nodes;     /* 0 */
+    unsigned num_qubits;        /* n (of the matrix, for a density matrix) */
+    uint64_t num_amps_per_node; /* 2^n, or 4^n for a density matrix */
+    unsigned log_num_amps_per_node;
+    int is_density_matrix;
+    int precision;
+} dfs_state_info;
+int dfs_state_get_info(dfs_state s, dfs_state_info* info);
+
+/* the device buffer (complex128 or complex64 interleaved, per precision) */
+int dfs_state_device_ptr(dfs_state s, void** ptr);
+
+/* host <-> device amplitude transfer of `count` amplitudes starting at `start`,
+ * interleaved doubles; replaces direct access to StateVector::amps and
+ * getAllVecAmps, tests/test_utilities.hpp:419-435 */
+int dfs_state_set_amps(dfs_state s, const double* amps, uint64_t start, uint64_t count);
+int dfs_state_get_amps(dfs_state s, double* amps, uint64_t start, uint64_t count);
+/* same, from/to host memory in the state's own device format (no conversion) */
+int dfs_state_set_raw(dfs_state s, const void* src, uint64_t start, uint64_t count);
+int dfs_state_get_raw(dfs_state s, void* dst, uint64_t start, uint64_t count);
+/* device-to-device copy between two states of equal shape and precision */
+int dfs_state_copy(dfs_state dst, dfs_state src);
+/* zero all amplitudes */
+int dfs_state_set_zero(dfs_state s);
+/* amps[index] = 1, all others 0 */
+int dfs_state_set_classical(dfs_state s, uint64_t index);
+/* seeded i.i.d. N(0,1) real and imaginary parts (counter-based generator;
+ * the same seed gives the same state on any GPU), optionally normalised to
+ * unit 2-norm.  Replaces setRandomAmps, tests/test_utilities.hpp:438-448. */
+int dfs_state_set_random(dfs_state s, uint64_t seed, int normalise);
+
+/* ------------------------------------------------------ statevector gates */
+/* All act on statevectors and, through the 2n-qubit view, on any state. */
+
+/* distributed_statevector_oneTargGate, src/distributed_statevector.hpp:18-40 */
+int dfs_statevector_oneTargGate(dfs_state s, unsigned target, const double* gate2x2);
+/* distributed_statevector_manyCtrlOneTargGate, src/distributed_statevector.hpp:81-106 */
+int dfs_statevector_manyCtrlOneTargGate(dfs_state s, const unsigned* controls, unsigned num_controls,
+                                        unsigned target, const double* gate2x2);
+/* distributed_statevector_swapGate, src/distributed_statevector.hpp:109-187 */
+int dfs_statevector_swapGate(dfs_state s, unsigned qb1, unsigned qb2);
+/* distributed_statevector_manyTargGate, src/distributed_statevector.hpp:190-224 */
+int dfs_statevector_manyTargGate(dfs_state s, const unsigned* targets, unsigned num_targets, const double* gate);
+/* distributed_statevector_pauliTensor, src/distributed_statevector.hpp:279-284 */
+int dfs_statevector_pauliTensor(dfs_state s, const unsigned* targets, const unsigned* paulis, unsigned num_targets);
+/* distributed_statevector_pauliGadget, src/distributed_statevector.hpp:287-292: exp(i theta P) */
+int dfs_statevector_pauliGadget(dfs_state s, const unsigned* targets, const unsigned* paulis, unsigned num_targets,
+                                double theta);
+/* distributed_statevector_phaseGadget, src/distributed_statevector.hpp:295-298: exp(i theta Z..Z) */
+int dfs_statevector_phaseGadget(dfs_state s, const unsigned* targets, unsigned num_targets, double theta);
+
+/* --------------------------------------------------- density-matrix calls */
+
+/* distributed_densitymatrix_manyTargGate, src/distributed_densitymatrix.hpp:15-25: rho -> U rho U^dagger */
+int dfs_densitymatrix_manyTargGate(dfs_state s, const unsigned* targets, unsigned num_targets, const double* gate);
+/* distributed_densitymatrix_swapGate, src/distributed_densitymatrix.hpp:28-33 */
+int dfs_densitymatrix_swapGate(dfs_state s, unsigned qb1, unsigned qb2);
+/* distributed_densitymatrix_pauliTensor, src/distributed_densitymatrix.hpp:36-50 */
+int dfs_densitymatrix_pauliTensor(dfs_state s, const unsigned* targets, const unsigned* paulis, unsigned num_targets);
+/* distributed_densitymatrix_pauliGadget, src/distributed_densitymatrix.hpp:53-64 */
+int dfs_densitymatrix_pauliGadget(dfs_state s, const unsigned* targets, const unsigned* paulis, unsigned num_targets,
+                                  double theta);
+/* distributed_densitymatrix_phaseGadget, src/distributed_densitymatrix.hpp:67-76 */
+int dfs_densitymatrix_phaseGadget(dfs_state s, const unsigned* targets, unsigned num_targets, double theta);
+/* distributed_densitymatrix_krausMap, src/distributed_densitymatrix.hpp:79-89: rho -> sum_i K_i rho K_i^dagger.
+ * kraus_ops holds num_ops row-major 2^k x 2^k complex matrices back to back. */
+int dfs_densitymatrix_krausMap(dfs_state s, const double* kraus_ops, unsigned num_ops, const unsigned* targets,
+                               unsigned num_targets);
+/* distributed_densitymatrix_oneQubitDephasing, src/distributed_densitymatrix.hpp:92-95 */
+int dfs_densitymatrix_oneQubitDephasing(dfs_state s, unsigned qb, double prob);
+/* distributed_densitymatrix_twoQubitDephasing, src/distributed_densitymatrix.hpp:98-101 */
+int dfs_densitymatrix_twoQubitDephasing(dfs_state s, unsigned qb1, unsigned qb2, double prob);
+/* distributed_densitymatrix_oneQubitDepolarising, src/distributed_densitymatrix.hpp:104-143 */
+int dfs_densitymatrix_oneQubitDepolarising(dfs_state s, unsigned qb, double prob);
+/* distributed_densitymatrix_twoQubitDepolarising, src/distributed_densitymatrix.hpp:241-263.
+ * Applies the trace-preserving channel (1-16p/15) rho + (4p/15) I (x) Tr_{qb1,qb2} rho that the
+ * reference's constants describe; the reference's own loop (src/local_densitymatrix.hpp:83-108)
+ * gives diagonal blocks an extra (4p/15) rho and is available through
+ * dfs_densitymatrix_twoQubitDepolarising_referenceCompat. */
+int dfs_densitymatrix_twoQubitDepolarising(dfs_state s, unsigned qb1, unsigned qb2, double prob);
+int dfs_densitymatrix_twoQubitDepolarising_referenceCompat(dfs_state s, unsigned qb1, unsigned qb2, double prob);
+/* distributed_densitymatrix_damping, src/distributed_densitymatrix.hpp:266-319 */
+int dfs_densitymatrix_damping(dfs_state s, unsigned qb, double prob);
+/* distributed_densitymatrix_expecPauliString, src/distributed_densitymatrix.hpp:322-344:
+ * sum_t coeffs[t] Tr(P_t rho); all_paulis holds num_terms rows of n codes (qubit q of term t
+ * at t*n + q).  The complex result is written to out_re, out_im. */
+int dfs_densitymatrix_expecPauliString(dfs_state s, const double* coeffs, unsigned num_terms,
+                                       const unsigned* all_paulis, double* out_re, double* out_im);
+/* distributed_densitymatrix_partialTrace, src/distributed_densitymatrix.hpp:347-406: creates the
+ * reduced density matrix of n - num_targets qubits (same precision) in *out */
+int dfs_densitymatrix_partialTrace(dfs_state s, const unsigned* targets, unsigned num_targets, dfs_state* out);
+
+/* ----------------------------------------------------------- additions */
+
+/* <psi| sum_t coeffs[t] P_t |psi> for a statevector (no reference counterpart; P_t is the
+ * operator distributed_statevector_pauliTensor applies), all_paulis as above. */
+int dfs_statevector_expecPauliSum(dfs_state s, const double* coeffs, unsigned num_terms,
+                                  const unsigned* all_paulis, double* out_re, double* out_im);
+/* <a|b> for two states of equal shape and precision */
+int dfs_state_inner_product(dfs_state a, dfs_state b, double* out_re, double* out_im);
+/* sum |amp|^2 */
+int dfs_state_norm_squared(dfs_state s, double* out);
+/* trace of a density matrix */
+int dfs_densitymatrix_trace(dfs_state s, double* out_re, double* out_im);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
