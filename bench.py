@@ -1,0 +1,460 @@
+"""Benchmark of the GB300 full-state engine (one JSON line on stdout).
+
+Workload: a 30-qubit complex128 statevector (16 GiB, seeded N(0,1) amplitudes,
+normalised) driven through a seeded 200-gate circuit drawn uniformly from the
+statevector gate mix (one-target Haar 2x2, two-control one-target, swap,
+three-target Haar 8x8, Pauli gadgets of weight 2..4, phase gadgets on 2..3
+qubits).  A step applies the whole circuit once; the metric is gates/s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+``--impl reference`` times the reference's own CPU code (built from its sources
+into oracle/_ref by ``__graft_entry__.build()``; the C restatement in oracle/
+when that is unavailable) on the host cores, on a bounded sample of the same
+circuit per step.  Under torchrun each rank drives one GPU with its own replica
+of the state (the path does not shard: replicas only); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "gates/s & HBM GB/s vs 8 TB/s @30q; adjoint grad/forward ratio; FP32 vs FP64 speedup"
+WORKLOAD = "sv30_c128_gate_mix"
+NUM_QUBITS = 30
+NUM_GATES = 200
+CIRCUIT_SEED = 20240611
+STATE_SEED = 77
+REF_SAMPLE_GATES = 6
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--qubits", type=int, default=NUM_QUBITS)
+    ap.add_argument("--gates", type=int, default=NUM_GATES)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the e2e, FP32 and native-FP64 legs")
+    return ap.parse_args()
+
+
+def load_modules():
+    import __graft_entry__ as ge
+    dfs = ge.package()
+    circuits = sys.modules.get("dfs_gb300.circuits")
+    if circuits is None:
+        import importlib
+        circuits = importlib.import_module("dfs_gb300.circuits")
+    return dfs, circuits
+
+
+# ----------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        sm, smax, reasons = [], 0.0, set()
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------- distributed bits
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def roofline_traffic(kind: str):
+    """dram read+write bytes per launch of `kind` from the committed ncu summary."""
+    f = ROOT / "profiles" / "ncu_sv30_gate_mix.md"
+    if not f.exists():
+        return None
+    m = re.search(rf"traffic_bytes_per_launch\[{re.escape(kind)}\]\s*=\s*([0-9.eE+]+)", f.read_text())
+    return float(m.group(1)) if m else None
+
+
+def measured_peak():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            return float(json.loads(f.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+# ------------------------------------------------------- reference arm
+
+def reference_arm(args, circuits):
+    """The reference's CPU implementation on the host cores, same workload."""
+    from oracle import build_oracle
+    from oracle.oracle import Oracle, Reference
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    os.environ.setdefault("OMP_PROC_BIND", "true")
+    os.environ.setdefault("OMP_WAIT_POLICY", "active")
+    n = args.qubits
+    gates = circuits.gate_mix(n, args.gates, CIRCUIT_SEED)
+    sample = gates[:REF_SAMPLE_GATES]
+    amps = seeded_host_state(n, STATE_SEED)
+    kind = "reference"
+    try:
+        backend = Reference()
+        h = backend.new_state(amps, False)
+        del amps
+
+        def run_gate(g):
+            run_reference_gate(backend, h, g)
+    except Exception:
+        kind = "port"
+        backend = Oracle()
+        h = None
+
+        def run_gate(g):
+            circuits.apply_to(backend, amps, [g])
+    for _ in range(args.warmup):
+        for g in sample:
+            run_gate(g)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for g in sample:
+            run_gate(g)
+    dt = time.perf_counter() - t0
+    if h is not None:
+        backend.free_state(h, False)
+    value = len(sample) * args.steps / dt
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "gates/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "qubits": n, "gates_per_step": len(sample),
+                   "sample": f"first {len(sample)} gates of the {args.gates}-gate circuit per step"},
+        "cpu_baseline": {"value": value, "unit": "gates/s", "cores": int(os.environ["OMP_NUM_THREADS"]),
+                         "kind": kind, "sample": f"first {len(sample)} gates of the circuit, {n} qubits"},
+        "e2e": {"value": value, "unit": "gates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def run_reference_gate(ref, h, g):
+    import ctypes as C
+    L = ref.lib
+
+    def u(xs):
+        xs = list(xs)
+        return (C.c_uint * max(1, len(xs)))(*xs), len(xs)
+
+    if g.kind in ("one_targ", "ctrl", "many_targ"):
+        m = np.ascontiguousarray(g.matrix, dtype=np.complex128)
+        mp = m.ctypes.data_as(C.c_void_p)
+    if g.kind == "one_targ":
+        L.ref_sv_one_targ(h, g.qubits[0], mp)
+    elif g.kind == "ctrl":
+        c, nc = u(g.controls)
+        L.ref_sv_many_ctrl_one_targ(h, c, nc, g.qubits[0], mp)
+    elif g.kind == "swap":
+        L.ref_sv_swap(h, g.qubits[0], g.qubits[1])
+    elif g.kind == "many_targ":
+        t, k = u(g.qubits)
+        L.ref_sv_many_targ(h, t, k, mp)
+    elif g.kind == "pauli_gadget":
+        t, k = u(g.qubits)
+        p, _ = u(g.paulis)
+        L.ref_sv_pauli_gadget(h, t, p, k, g.param)
+    elif g.kind == "phase_gadget":
+        t, k = u(g.qubits)
+        L.ref_sv_phase_gadget(h, t, k, g.param)
+    else:
+        raise ValueError(g.kind)
+
+
+def seeded_host_state(n, seed):
+    """N(0,1) real and imaginary parts, normalised, generated on the host in
+    parallel chunks (numpy releases the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+    N = 1 << n
+    out = np.empty(N, dtype=np.complex128)
+    view = out.view(np.float64)
+    chunks = max(1, min(64, N >> 20))
+    seqs = np.random.SeedSequence(seed).spawn(chunks)
+    step = (2 * N) // chunks
+
+    def fill(i):
+        np.random.default_rng(seqs[i]).standard_normal(out=view[i * step:(i + 1) * step])
+        return float(np.dot(view[i * step:(i + 1) * step], view[i * step:(i + 1) * step]))
+
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        total = sum(ex.map(fill, range(chunks)))
+    out *= 1.0 / np.sqrt(total)
+    return out
+
+
+# ------------------------------------------------------------- GPU arm
+
+def gpu_arm(args, world, rank, local):
+    import torch
+    dfs, circuits = load_modules()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as td
+        td.init_process_group("nccl", device_id=torch.device("cuda", local))
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    dfs.comm_init()
+    dfs.set_stream(stream)
+    n = args.qubits
+    gates = circuits.gate_mix(n, args.gates, CIRCUIT_SEED)
+    elem = 16
+    num_amps = 1 << n
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as td
+            td.barrier()
+
+    psi = dfs.StateVector(n, precision="c128")
+    psi.setRandomAmps(seed=STATE_SEED, normalise=True)
+
+    # warm-up
+    for _ in range(args.warmup):
+        circuits.apply(dfs, psi, gates)
+
+    # timed region: per-gate events on the engine stream for the kernel breakdown
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(len(gates) * args.steps)]
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    start.record(stream)
+    i = 0
+    for _ in range(args.steps):
+        for g in gates:
+            evs[i][0].record(stream)
+            circuits.apply(dfs, psi, [g])
+            evs[i][1].record(stream)
+            i += 1
+    stop.record(stream)
+    barrier()
+    clock_info = clocks.stop()
+    elapsed_ms = start.elapsed_time(stop)
+    if world > 1:
+        import torch.distributed as td
+        t = torch.tensor([elapsed_ms], device="cuda")
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    total_gates = len(gates) * args.steps
+    value = world * total_gates / (elapsed_ms / 1e3)
+
+    per_kind = {}
+    for j, (a, b) in enumerate(evs):
+        g = gates[j % len(gates)]
+        d = per_kind.setdefault(g.kind, {"ms": 0.0, "launches": 0, "bytes": 0})
+        d["ms"] += a.elapsed_time(b)
+        d["launches"] += circuits.kernel_launches(g)
+        d["bytes"] += circuits.algorithmic_bytes(g, num_amps, elem)
+    kernel_ms = sum(d["ms"] for d in per_kind.values())
+    kernels = {}
+    for kind, d in per_kind.items():
+        kernels[kind] = {"launches": d["launches"], "ms_avg": d["ms"] / d["launches"],
+                         "share": d["ms"] / kernel_ms, "gbs": d["bytes"] / (d["ms"] * 1e-3) / 1e9}
+    dominant = max(kernels, key=lambda k: kernels[k]["share"])
+    peak, peak_kind = measured_peak()
+    dom_bytes = per_kind[dominant]["bytes"] / per_kind[dominant]["launches"]
+    achieved = kernels[dominant]["gbs"]
+    all_bytes = sum(d["bytes"] for d in per_kind.values())
+    algo_gbs = all_bytes / (elapsed_ms * 1e-3) / 1e9
+
+    result = {
+        "metric": METRIC, "value": value, "unit": "gates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "arith": "IEEE f64 storage; double-float (2 x f32, >= 47-bit) arithmetic on the FP32 pipes",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "qubits": n, "gates_per_step": len(gates), "precision": "c128",
+                   "circuit_seed": CIRCUIT_SEED, "state": "seeded N(0,1), normalised, device generator",
+                   "l2": "state 16 GiB > L2 129 MB: no flush needed", "parallelism": f"replicas x{world}"},
+        "hbm_gbs_algorithmic": algo_gbs,
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": roofline_traffic(dominant), "algorithmic_bytes_per_launch": dom_bytes},
+        "kernels": kernels,
+        "gpu_launches": sum(d["launches"] for d in per_kind.values()),
+        "clocks": clock_info,
+    }
+
+    if not args.no_extras:
+        # end to end through the C ABI with host buffers: upload the step's input
+        # state from pinned memory, run the circuit, read the final state back
+        host = torch.empty(num_amps * 2, dtype=torch.float64, pin_memory=True)
+        hv = host.numpy()
+        import ctypes as C
+        ptr = hv.ctypes.data_as(C.POINTER(C.c_double))
+        lib = dfs.load_library()
+        lib.dfs_state_get_amps(psi.handle, ptr, 0, num_amps)  # a valid input state
+        e2e_steps = max(1, min(2, args.steps))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            assert lib.dfs_state_set_amps(psi.handle, ptr, 0, num_amps) == 0
+            circuits.apply(dfs, psi, gates)
+            assert lib.dfs_state_get_amps(psi.handle, ptr, 0, num_amps) == 0
+        barrier()
+        e2e_s = time.perf_counter() - t0
+        result["e2e"] = {"value": world * len(gates) * e2e_steps / e2e_s, "unit": "gates/s",
+                         "h2d_bytes_per_step": num_amps * elem, "d2h_bytes_per_step": num_amps * elem}
+        del host, hv
+        psi.free()
+
+        # FP32 form: the same circuit on a complex64 state
+        phi = dfs.StateVector(n, precision="c64")
+        phi.setRandomAmps(seed=STATE_SEED, normalise=True)
+        circuits.apply(dfs, phi, gates)
+        barrier()
+        t0 = time.perf_counter()
+        f32_steps = max(1, min(3, args.steps))
+        for _ in range(f32_steps):
+            circuits.apply(dfs, phi, gates)
+        barrier()
+        f32 = len(gates) * f32_steps / (time.perf_counter() - t0)
+        phi.free()
+        # native FP64 arithmetic: the same circuit, IEEE double FMA (1.2 TFLOP/s on GB300)
+        nat = dfs.StateVector(n, precision="c128_native")
+        nat.setRandomAmps(seed=STATE_SEED, normalise=True)
+        circuits.apply(dfs, nat, gates[:20])
+        barrier()
+        t0 = time.perf_counter()
+        circuits.apply(dfs, nat, gates)
+        barrier()
+        native = len(gates) / (time.perf_counter() - t0)
+        nat.free()
+        per_gpu = value / world
+        result["fp32"] = {"gates_per_s": f32, "speedup_vs_f64": f32 / per_gpu}
+        result["f64_native"] = {"gates_per_s": native, "emulated_speedup": per_gpu / native}
+    else:
+        psi.free()
+
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(args, circuits, gates)
+    return result, rank
+
+
+def cpu_baseline(args, circuits, gates):
+    """The reference's CPU code (oracle/_ref) on the host cores: the first
+    REF_SAMPLE_GATES gates of the same circuit on the same-size state."""
+    try:
+        from oracle.oracle import Oracle, Reference
+    except Exception as e:  # pragma: no cover
+        return {"value": None, "error": str(e)}
+    cores = os.cpu_count() or 1
+    n = args.qubits
+    sample = gates[:REF_SAMPLE_GATES]
+    amps = seeded_host_state(n, STATE_SEED)
+    try:
+        ref = Reference()
+        kind = "reference"
+    except Exception:
+        ref = None
+        kind = "port"
+    if ref is not None:
+        h = ref.new_state(amps, False)
+        del amps
+        t0 = time.perf_counter()
+        for g in sample:
+            run_reference_gate(ref, h, g)
+        dt = time.perf_counter() - t0
+        ref.free_state(h, False)
+    else:
+        orc = Oracle()
+        t0 = time.perf_counter()
+        circuits.apply_to(orc, amps, sample)
+        dt = time.perf_counter() - t0
+    return {"value": len(sample) / dt, "unit": "gates/s", "cores": int(os.environ.get("OMP_NUM_THREADS", cores)),
+            "kind": kind, "sample": f"first {len(sample)} gates of the circuit on the {n}-qubit state"}
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+        _, circuits = load_modules()
+        print(json.dumps(reference_arm(args, circuits)), flush=True)
+        return
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    result, rank = gpu_arm(args, world, rank, local)
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        import torch.distributed as td
+        td.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,221 @@
+"""Seeded synthetic circuits for the benchmark configurations.
+
+There is no public dataset for this path: every workload is drawn from a
+seeded ``numpy.random.Generator`` with the shapes and distributions of the
+engine's benchmark configurations:
+
+* ``gate_mix``: gates drawn uniformly from one-target Haar 2x2 unitaries,
+  2-control one-target gates, swaps, 3-target Haar 8x8 unitaries, Pauli gadgets
+  on random weight-2..4 strings with theta ~ U[0, 2 pi), and phase gadgets on
+  2..3 qubits (optionally also k = 2..6 dense Haar gates);
+* ``dm_layers``: layers of 2-target Haar unitaries each followed by one/two
+  qubit dephasing, depolarising and damping with prob ~ U[0, 0.1];
+* ``pauli_sum``: random Pauli strings with N(0,1) coefficients.
+
+A circuit is a list of ``Gate`` tuples; ``apply`` runs one through the engine's
+reference-named API.  Pauli strings that would be all-Z are resampled, as the
+reference's tests do (tests/test_utilities.hpp:218-224).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Sequence
+
+import numpy as np
+
+GATE_KINDS = ("one_targ", "ctrl", "swap", "many_targ", "pauli_gadget", "phase_gadget")
+DM_KINDS = ("dm_many_targ", "deph1", "deph2", "depol1", "depol2", "damping")
+
+
+@dataclass
+class Gate:
+    kind: str
+    qubits: tuple = ()
+    controls: tuple = ()
+    matrix: np.ndarray | None = None
+    paulis: tuple = ()
+    param: float = 0.0
+
+    @property
+    def num_targets(self) -> int:
+        return len(self.qubits)
+
+
+def haar_unitary(rng: np.random.Generator, d: int) -> np.ndarray:
+    """QR of a complex Ginibre matrix with R's diagonal phases moved into Q (Mezzadri 2007)."""
+    z = (rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))) / np.sqrt(2.0)
+    q, r = np.linalg.qr(z)
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+def random_pauli_string(rng: np.random.Generator, num_qubits: int, weight: int):
+    targets = tuple(int(q) for q in rng.choice(num_qubits, size=weight, replace=False))
+    paulis = [int(p) for p in rng.integers(1, 4, size=weight)]
+    if all(p == 3 for p in paulis):
+        paulis[0] = int(rng.integers(1, 3))
+    return targets, tuple(paulis)
+
+
+def gate_mix(num_qubits: int, num_gates: int, seed: int, dense_k: Sequence[int] = ()) -> list[Gate]:
+    """The statevector gate mix; ``dense_k`` adds k-target Haar gates as extra kinds."""
+    rng = np.random.default_rng(seed)
+    kinds = list(GATE_KINDS) + [f"dense{k}" for k in dense_k]
+    gates = []
+    for _ in range(num_gates):
+        kind = kinds[int(rng.integers(len(kinds)))]
+        if kind == "one_targ":
+            gates.append(Gate("one_targ", (int(rng.integers(num_qubits)),), matrix=haar_unitary(rng, 2)))
+        elif kind == "ctrl":
+            q = [int(x) for x in rng.choice(num_qubits, size=3, replace=False)]
+            gates.append(Gate("ctrl", (q[0],), controls=(q[1], q[2]), matrix=haar_unitary(rng, 2)))
+        elif kind == "swap":
+            q = [int(x) for x in rng.choice(num_qubits, size=2, replace=False)]
+            gates.append(Gate("swap", tuple(q)))
+        elif kind == "many_targ":
+            q = tuple(int(x) for x in rng.choice(num_qubits, size=3, replace=False))
+            gates.append(Gate("many_targ", q, matrix=haar_unitary(rng, 8)))
+        elif kind == "pauli_gadget":
+            t, p = random_pauli_string(rng, num_qubits, int(rng.integers(2, 5)))
+            gates.append(Gate("pauli_gadget", t, paulis=p, param=float(rng.uniform(0, 2 * np.pi))))
+        elif kind == "phase_gadget":
+            q = tuple(int(x) for x in rng.choice(num_qubits, size=int(rng.integers(2, 4)), replace=False))
+            gates.append(Gate("phase_gadget", q, param=float(rng.uniform(0, 2 * np.pi))))
+        else:
+            k = int(kind[5:])
+            q = tuple(int(x) for x in rng.choice(num_qubits, size=k, replace=False))
+            gates.append(Gate("many_targ", q, matrix=haar_unitary(rng, 1 << k)))
+    return gates
+
+
+def dm_layers(num_qubits: int, num_layers: int, seed: int, max_prob: float = 0.1) -> list[Gate]:
+    """Layers of a 2-target Haar unitary on a random pair followed by one/two-qubit
+    dephasing, depolarising and damping with prob ~ U[0, max_prob]."""
+    rng = np.random.default_rng(seed)
+    ops = []
+    for _ in range(num_layers):
+        pair = tuple(int(x) for x in rng.choice(num_qubits, size=2, replace=False))
+        ops.append(Gate("dm_many_targ", pair, matrix=haar_unitary(rng, 4)))
+
+        def p():
+            return float(rng.uniform(0, max_prob))
+
+        def q1():
+            return (int(rng.integers(num_qubits)),)
+
+        def q2():
+            return tuple(int(x) for x in rng.choice(num_qubits, size=2, replace=False))
+
+        ops.append(Gate("deph1", q1(), param=p()))
+        ops.append(Gate("deph2", q2(), param=p()))
+        ops.append(Gate("depol1", q1(), param=p()))
+        ops.append(Gate("depol2", q2(), param=p()))
+        ops.append(Gate("damping", q1(), param=p()))
+    return ops
+
+
+def pauli_sum(num_qubits: int, num_terms: int, seed: int):
+    """(coeffs, codes): N(0,1) coefficients and uniform codes 0..3, one row per term."""
+    rng = np.random.default_rng(seed)
+    return rng.normal(size=num_terms), rng.integers(0, 4, size=(num_terms, num_qubits)).astype(np.uint32)
+
+
+def gadget_ansatz(num_qubits: int, layers: int, per_layer: int, seed: int) -> list[Gate]:
+    """Layers of Pauli gadgets on random weight-2..4 strings with theta ~ N(0, 1)."""
+    rng = np.random.default_rng(seed)
+    gates = []
+    for _ in range(layers * per_layer):
+        t, p = random_pauli_string(rng, num_qubits, int(rng.integers(2, 5)))
+        gates.append(Gate("pauli_gadget", t, paulis=p, param=float(rng.normal())))
+    return gates
+
+
+# ------------------------------------------------------------- application
+
+def apply(dfs, state, gates: Sequence[Gate]) -> None:
+    """Run a circuit through the engine's reference-named API."""
+    for g in gates:
+        k = g.kind
+        if k == "one_targ":
+            dfs.distributed_statevector_oneTargGate(state, g.qubits[0], g.matrix)
+        elif k == "ctrl":
+            dfs.distributed_statevector_manyCtrlOneTargGate(state, g.controls, g.qubits[0], g.matrix)
+        elif k == "swap":
+            dfs.distributed_statevector_swapGate(state, g.qubits[0], g.qubits[1])
+        elif k == "many_targ":
+            dfs.distributed_statevector_manyTargGate(state, g.qubits, g.matrix)
+        elif k == "pauli_gadget":
+            dfs.distributed_statevector_pauliGadget(state, g.qubits, g.paulis, g.param)
+        elif k == "pauli_tensor":
+            dfs.distributed_statevector_pauliTensor(state, g.qubits, g.paulis)
+        elif k == "phase_gadget":
+            dfs.distributed_statevector_phaseGadget(state, g.qubits, g.param)
+        elif k == "dm_many_targ":
+            dfs.distributed_densitymatrix_manyTargGate(state, g.qubits, g.matrix)
+        elif k == "deph1":
+            dfs.distributed_densitymatrix_oneQubitDephasing(state, g.qubits[0], g.param)
+        elif k == "deph2":
+            dfs.distributed_densitymatrix_twoQubitDephasing(state, g.qubits[0], g.qubits[1], g.param)
+        elif k == "depol1":
+            dfs.distributed_densitymatrix_oneQubitDepolarising(state, g.qubits[0], g.param)
+        elif k == "depol2":
+            dfs.distributed_densitymatrix_twoQubitDepolarising(state, g.qubits[0], g.qubits[1], g.param)
+        elif k == "damping":
+            dfs.distributed_densitymatrix_damping(state, g.qubits[0], g.param)
+        else:
+            raise ValueError(f"unknown gate kind {k}")
+
+
+def apply_to(backend, amps: np.ndarray, gates: Sequence[Gate]) -> None:
+    """Run a circuit through an object with the oracle's method names
+    (``sv_one_targ(amps, ...)`` etc.), e.g. the parity checker."""
+    for g in gates:
+        k = g.kind
+        if k == "one_targ":
+            backend.sv_one_targ(amps, g.qubits[0], g.matrix)
+        elif k == "ctrl":
+            backend.sv_many_ctrl_one_targ(amps, g.controls, g.qubits[0], g.matrix)
+        elif k == "swap":
+            backend.sv_swap(amps, g.qubits[0], g.qubits[1])
+        elif k == "many_targ":
+            backend.sv_many_targ(amps, g.qubits, g.matrix)
+        elif k == "pauli_gadget":
+            backend.sv_pauli_gadget(amps, g.qubits, g.paulis, g.param)
+        elif k == "pauli_tensor":
+            backend.sv_pauli_tensor(amps, g.qubits, g.paulis)
+        elif k == "phase_gadget":
+            backend.sv_phase_gadget(amps, g.qubits, g.param)
+        elif k == "dm_many_targ":
+            backend.dm_many_targ(amps, g.qubits, g.matrix)
+        elif k == "deph1":
+            backend.dm_deph1(amps, g.qubits[0], g.param)
+        elif k == "deph2":
+            backend.dm_deph2(amps, g.qubits[0], g.qubits[1], g.param)
+        elif k == "depol1":
+            backend.dm_depol1(amps, g.qubits[0], g.param)
+        elif k == "depol2":
+            backend.dm_depol2(amps, g.qubits[0], g.qubits[1], g.param)
+        elif k == "damping":
+            backend.dm_damping(amps, g.qubits[0], g.param)
+        else:
+            raise ValueError(f"unknown gate kind {k}")
+
+
+def algorithmic_bytes(g: Gate, num_amps: int, elem_bytes: int) -> int:
+    """Bytes a kernel must move for one gate: read + write of the amplitudes it
+    can change (full state for dense, pair and diagonal sweeps; 1/2^c of it for c
+    controls; half of it read and written for a swap)."""
+    full = 2 * num_amps * elem_bytes
+    if g.kind == "ctrl":
+        return full >> len(g.controls)
+    if g.kind == "swap":
+        return num_amps * elem_bytes
+    if g.kind == "deph1":
+        return num_amps * elem_bytes
+    if g.kind == "dm_many_targ":
+        return 2 * full
+    return full
+
+
+def kernel_launches(g: Gate) -> int:
+    """Engine kernel launches issued for one gate."""
+    return 2 if g.kind == "dm_many_targ" else 1
