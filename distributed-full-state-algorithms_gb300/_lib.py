@@ -109,6 +109,7 @@ PROTOTYPES = {
     "dfs_state_inner_product": [_H, _H, _DP, _DP],
     "dfs_state_norm_squared": [_H, _DP],
     "dfs_densitymatrix_trace": [_H, _DP, _DP],
+    "dfs_densitymatrix_expecPauliString_noalloc": [_H, _DP, _U, _UP, _DP, _DP],
     "dfs_error_string": [_I],
     "dfs_last_error": [],
 }

@@ -197,6 +197,22 @@ int dfs_state_norm_squared(dfs_state s, double* out);
 /* trace of a density matrix */
 int dfs_densitymatrix_trace(dfs_state s, double* out_re, double* out_im);
 
+/* dfs_densitymatrix_expecPauliString without any memory allocation.  No counterpart in the
+ * reference.  For callers that cannot allocate at the point of the call: code whose device
+ * memory is owned by a pool or caching allocator, loops that cannot afford the device
+ * synchronisation cudaFree implies, and call sites captured into CUDA graphs.  The ordinary
+ * entry point grows a device scratch buffer and pinned host staging on demand; this one keeps
+ * its partial sums in a fixed 128 KiB device array (8192 complex slots) compiled into the
+ * library, which every GPU that loads the library holds until the process exits.  A call on an
+ * n-qubit matrix needs num_terms * chunks + 1 slots, chunks = ceil(2^n / max(4096, 2^n/256))
+ * (1 for n <= 12); larger requests return DFS_ERR_TOO_LARGE.  All calls share the array: each
+ * call writes every slot it reads, but calls that overlap on the GPU (other streams or threads)
+ * race and must be serialised by the caller.  The first call on each device looks the array's
+ * address up with cudaGetSymbolAddress, so make it before any stream capture begins.  Results
+ * equal dfs_densitymatrix_expecPauliString's within rounding. */
+int dfs_densitymatrix_expecPauliString_noalloc(dfs_state s, const double* coeffs, unsigned num_terms,
+                                               const unsigned* all_paulis, double* out_re, double* out_im);
+
 #ifdef __cplusplus
 }
 #endif
