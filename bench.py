@@ -128,6 +128,20 @@ def dist_setup(args):
     return world, rank, local
 
 
+def replica_throughput(local_ms: float, units_per_rank: int, world: int, device="cpu") -> tuple[float, float]:
+    """Whole-job throughput of independent replicas: every rank processed
+    `units_per_rank` units; the job took as long as the slowest rank.
+    Returns (units per second over all ranks, max elapsed ms)."""
+    ms = local_ms
+    if world > 1:
+        import torch
+        import torch.distributed as td
+        t = torch.tensor([local_ms], dtype=torch.float64, device=device)
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+        ms = float(t.item())
+    return world * units_per_rank / (ms / 1e3), ms
+
+
 def roofline_traffic(kind: str):
     """dram read+write bytes per launch of `kind` from the committed ncu summary."""
     f = ROOT / "profiles" / "ncu_sv30_gate_mix.md"
@@ -301,14 +315,8 @@ def gpu_arm(args, world, rank, local):
     stop.record(stream)
     barrier()
     clock_info = clocks.stop()
-    elapsed_ms = start.elapsed_time(stop)
-    if world > 1:
-        import torch.distributed as td
-        t = torch.tensor([elapsed_ms], device="cuda")
-        td.all_reduce(t, op=td.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
     total_gates = len(gates) * args.steps
-    value = world * total_gates / (elapsed_ms / 1e3)
+    value, elapsed_ms = replica_throughput(start.elapsed_time(stop), total_gates, world, device="cuda")
 
     per_kind = {}
     for j, (a, b) in enumerate(evs):
