@@ -47,7 +47,7 @@ def _newer(target: Path, deps: list[Path]) -> bool:
 def build(force: bool = False, verbose: bool = True, extra_flags: list[str] | None = None) -> Path:
     BUILD.mkdir(exist_ok=True)
     hdrs = headers()
-    flags = NVCC_FLAGS + (extra_flags or [])
+    flags = NVCC_FLAGS + (extra_flags or []) + os.environ.get("DFS_NVCC_FLAGS", "").split()
     procs = []
     objs = []
     for src in sources():

@@ -36,7 +36,7 @@ struct RunDeph1 {
     static int run(State* s, unsigned q, double p) {
         Deph1Op<P, IT> op{P::mkr(1 - 2 * p), (int)q, (int)(q + s->numQubits)};
         IT items = (IT)(s->numAmps / 4);
-        return launch(k_pair<P, IT, Deph1Op<P, IT>>, items, kPer, "oneQubitDephasing", (typename P::store*)s->amps,
+        return launch(k_pair<P, IT, Deph1Op<P, IT>>, items, pair_per<P>(), "oneQubitDephasing", (typename P::store*)s->amps,
                       items, op);
     }
 };
@@ -60,7 +60,7 @@ struct RunDeph2 {
         unsigned n = s->numQubits;
         Deph2Op<P, IT> op{P::mkr(1 - 4 * p / 3), (int)q1, (int)(q1 + n), (int)q2, (int)(q2 + n)};
         IT items = (IT)s->numAmps;
-        return launch(k_diag<P, IT, Deph2Op<P, IT>>, items, 4, "twoQubitDephasing", (typename P::store*)s->amps,
+        return launch(k_diag<P, IT, Deph2Op<P, IT>>, items, diag_per<P>(), "twoQubitDephasing", (typename P::store*)s->amps,
                       items, op);
     }
 };
@@ -71,6 +71,7 @@ int dm_deph2(State* s, unsigned q1, unsigned q2, double p) { return dispatch<Run
 
 template <class P, class IT, class Op>
 __global__ void __launch_bounds__(kThreads) k_quad(typename P::store* __restrict__ a, IT items, int q, int qa, Op op) {
+    constexpr int kPer = pair_per<P>();
     const IT stride = (IT)gridDim.x * (IT)(kThreads * kPer);
     const IT bq = (IT)1 << q, ba = (IT)1 << qa;
     for (IT base = (IT)blockIdx.x * (IT)(kThreads * kPer) + threadIdx.x; base < items; base += stride) {
@@ -137,7 +138,7 @@ struct RunDepol1 {
     static int run(State* s, unsigned q, double p) {
         Depol1Op<P> op{P::mkr(2 * p / 3), P::mkr(1 - 2 * p / 3), P::mkr(1 - 4 * p / 3)};
         IT items = (IT)(s->numAmps / 4);
-        return launch(k_quad<P, IT, Depol1Op<P>>, items, kPer, "oneQubitDepolarising", (typename P::store*)s->amps,
+        return launch(k_quad<P, IT, Depol1Op<P>>, items, pair_per<P>(), "oneQubitDepolarising", (typename P::store*)s->amps,
                       items, (int)q, (int)(q + s->numQubits), op);
     }
 };
@@ -148,7 +149,7 @@ struct RunDamping {
     static int run(State* s, unsigned q, double p) {
         DampingOp<P> op{P::mkr(p), P::mkr(std::sqrt(1 - p)), P::mkr(1 - p)};
         IT items = (IT)(s->numAmps / 4);
-        return launch(k_quad<P, IT, DampingOp<P>>, items, kPer, "damping", (typename P::store*)s->amps, items, (int)q,
+        return launch(k_quad<P, IT, DampingOp<P>>, items, pair_per<P>(), "damping", (typename P::store*)s->amps, items, (int)q,
                       (int)(q + s->numQubits), op);
     }
 };

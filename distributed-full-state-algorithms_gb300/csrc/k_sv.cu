@@ -42,7 +42,7 @@ struct RunOneTarg {
         op.t = (int)t;
         for (int i = 0; i < 4; i++) op.g[i] = P::mk(g[2 * i], g[2 * i + 1]);
         IT items = (IT)(s->numAmps / 2);
-        return launch(k_pair<P, IT, OneTargOp<P, IT>>, items, kPer, "oneTargGate", (typename P::store*)s->amps,
+        return launch(k_pair<P, IT, OneTargOp<P, IT>>, items, pair_per<P>(), "oneTargGate", (typename P::store*)s->amps,
                       items, op);
     }
 };
@@ -84,7 +84,7 @@ struct RunCtrlOneTarg {
         op.tbit = (IT)(1ull << t);
         for (int i = 0; i < 4; i++) op.g[i] = P::mk(g[2 * i], g[2 * i + 1]);
         IT items = (IT)(s->numAmps >> (nc + 1));
-        return launch(k_pair<P, IT, CtrlOneTargOp<P, IT>>, items, kPer, "manyCtrlOneTargGate",
+        return launch(k_pair<P, IT, CtrlOneTargOp<P, IT>>, items, pair_per<P>(), "manyCtrlOneTargGate",
                       (typename P::store*)s->amps, items, op);
     }
 };
@@ -118,7 +118,7 @@ struct RunSwap {
         SwapOp<IT> op{(int)std::min(q1, q2), (int)std::max(q1, q2)};
         IT items = (IT)(s->numAmps / 4);
         using S = typename P::store;
-        return launch(k_pair_raw<S, IT, SwapOp<IT>>, items, kPer, "swapGate", (S*)s->amps, items, op);
+        return launch(k_pair_raw<S, IT, SwapOp<IT>>, items, kRawPairPer, "swapGate", (S*)s->amps, items, op);
     }
 };
 int sv_swap(State* s, unsigned q1, unsigned q2) { return dispatch<RunSwap>(s, s, q1, q2); }
@@ -203,20 +203,20 @@ struct RunPauli {
             if (!gadget) {
                 if (mYZ == 0) return DFS_SUCCESS;  // identity
                 DiagSignOp<IT> op{(IT)mYZ};
-                return launch(k_diag_raw<S, IT, DiagSignOp<IT>>, items, 4, "pauliTensor", (S*)s->amps, items, op);
+                return launch(k_diag_raw<S, IT, DiagSignOp<IT>>, items, kRawDiagPer, "pauliTensor", (S*)s->amps, items, op);
             }
             // exp(i theta Z..Z): e^{+i theta} on even parity, e^{-i theta} on odd
             DiagPhaseOp<P, IT> op;
             op.k0 = P::mk(std::cos(theta), std::sin(theta));
             op.k1 = P::mk(std::cos(theta), -std::sin(theta));
             op.mask = (IT)mYZ;
-            return launch(k_diag<P, IT, DiagPhaseOp<P, IT>>, items, 4, "pauliGadget", (typename P::store*)s->amps,
+            return launch(k_diag<P, IT, DiagPhaseOp<P, IT>>, items, diag_per<P>(), "pauliGadget", (typename P::store*)s->amps,
                           items, op);
         }
         IT items = (IT)(s->numAmps / 2);
         if (!gadget) {
             PauliTensorOp<IT> op{(IT)mX, (IT)mYZ, top, numY & 3};
-            return launch(k_pair_raw<S, IT, PauliTensorOp<IT>>, items, kPer, "pauliTensor", (S*)s->amps, items, op);
+            return launch(k_pair_raw<S, IT, PauliTensorOp<IT>>, items, kRawPairPer, "pauliTensor", (S*)s->amps, items, op);
         }
         PauliGadgetOp<P, IT> op;
         op.c = P::mkr(std::cos(theta));
@@ -225,7 +225,7 @@ struct RunPauli {
         op.maskYZ = (IT)mYZ;
         op.top = top;
         op.powY = (numY + 1) & 3;
-        return launch(k_pair<P, IT, PauliGadgetOp<P, IT>>, items, kPer, "pauliGadget", (typename P::store*)s->amps,
+        return launch(k_pair<P, IT, PauliGadgetOp<P, IT>>, items, pair_per<P>(), "pauliGadget", (typename P::store*)s->amps,
                       items, op);
     }
 };
@@ -246,7 +246,7 @@ struct RunPhaseGadget {
         op.k1 = P::mk(std::cos(theta), -std::sin(theta));
         op.mask = (IT)m;
         IT items = (IT)s->numAmps;
-        return launch(k_diag<P, IT, DiagPhaseOp<P, IT>>, items, 4, "phaseGadget", (typename P::store*)s->amps, items,
+        return launch(k_diag<P, IT, DiagPhaseOp<P, IT>>, items, diag_per<P>(), "phaseGadget", (typename P::store*)s->amps, items,
                       op);
     }
 };
@@ -274,10 +274,10 @@ struct RunScale {
         IT items = (IT)s->numAmps;
         if (f == -1.0) {
             using S = typename P::store;
-            return launch(k_diag_raw<S, IT, NegateOp<IT>>, items, 4, "negate", (S*)s->amps, items, NegateOp<IT>{});
+            return launch(k_diag_raw<S, IT, NegateOp<IT>>, items, kRawDiagPer, "negate", (S*)s->amps, items, NegateOp<IT>{});
         }
         ScaleOp<P, IT> op{P::mkr(f)};
-        return launch(k_diag<P, IT, ScaleOp<P, IT>>, items, 4, "scale", (typename P::store*)s->amps, items, op);
+        return launch(k_diag<P, IT, ScaleOp<P, IT>>, items, diag_per<P>(), "scale", (typename P::store*)s->amps, items, op);
     }
 };
 int state_scale_real(State* s, double factor) { return dispatch<RunScale>(s, s, factor); }
@@ -299,18 +299,26 @@ template <class P, class IT, int K>
 __global__ void __launch_bounds__(kThreads) k_many_targ_reg(typename P::store* __restrict__ a, IT items,
                                                             ManyTargRegOp<P, IT, K> op) {
     constexpr int D = 1 << K;
+    // the gate and offsets are staged in shared memory so that the row loop can
+    // stay rolled: a fully unrolled D x D double-float product overflows the
+    // instruction cache (ncu: no_instruction stalls dominate)
+    __shared__ typename P::K g[D][D];
+    __shared__ IT off[D];
+    for (int e = threadIdx.x; e < D * D; e += kThreads) g[e / D][e % D] = op.g[e / D][e % D];
+    for (int e = threadIdx.x; e < D; e += kThreads) off[e] = op.off[e];
+    __syncthreads();
     const IT stride = (IT)gridDim.x * kThreads;
     for (IT j = (IT)blockIdx.x * kThreads + threadIdx.x; j < items; j += stride) {
         IT b = insert_zeros(j, op.q);
         typename P::V x[D];
 #pragma unroll
-        for (int c = 0; c < D; c++) x[c] = P::load(a, b + op.off[c]);
-#pragma unroll
+        for (int c = 0; c < D; c++) x[c] = P::load(a, b + off[c]);
+#pragma unroll(K >= 3 ? 1 : D)
         for (int r = 0; r < D; r++) {
-            typename P::A acc = P::first(op.g[r][0], x[0]);
+            typename P::A acc = P::first(g[r][0], x[0]);
 #pragma unroll
-            for (int c = 1; c < D; c++) P::mac(acc, op.g[r][c], x[c]);
-            P::save(a, b + op.off[r], P::get(acc));
+            for (int c = 1; c < D; c++) P::mac(acc, g[r][c], x[c]);
+            P::save(a, b + off[r], P::get(acc));
         }
     }
 }
