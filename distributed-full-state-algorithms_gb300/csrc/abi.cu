@@ -8,6 +8,7 @@
 #include <complex>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -60,6 +61,8 @@ static int ensure_init() {
     g_ctx.stream = g_ctx.ownStream;
     e = cudaEventCreateWithFlags(&g_ctx.pinnedFree, cudaEventDisableTiming);
     if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+    const char* tcEnv = getenv("DFS_DENSE_TC");
+    g_ctx.denseTensorCores = !(tcEnv && tcEnv[0] == '0');
     g_ctx.initialised = true;
     return DFS_SUCCESS;
 }
@@ -241,7 +244,8 @@ int dfs_comm_synch(void) {
     int rc = ensure_init();
     if (rc) return rc;
     cudaError_t e = cudaStreamSynchronize(g_ctx.stream);
-    return e == cudaSuccess ? DFS_SUCCESS : cuda_fail(e, "comm_synch");
+    if (e != cudaSuccess) return cuda_fail(e, "comm_synch");
+    return dense_tc_status();
 }
 
 int dfs_set_stream(void* stream) {

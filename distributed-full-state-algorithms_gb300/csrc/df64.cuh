@@ -160,6 +160,32 @@ DF_HD void encode_words(f2 v, uint32_t* H, uint32_t* L) {
     *L = tiny ? 0u : Lr;
 }
 
+// encode_words for the value (hi + lo) * 2^shift: the shift goes into the
+// exponent field (used when a double-float result carries an external power of
+// two); a result below the double normal range is flushed to a signed zero.
+DF_HD void encode_words_scaled(f2 v, int shift, uint32_t* H, uint32_t* L) {
+    uint32_t hb = fbits(v.hi);
+    uint32_t fe = hb & 0x7F800000u;
+    int ebias = 896 + shift;
+    uint32_t Hh = ((hb & 0x7FFFFFFFu) >> 3) + (uint32_t)(ebias << 20);
+    uint32_t Lh = hb << 29;
+    uint32_t sb = (306u << 23) - (hb & 0xFF800000u);
+    float scaled = mul_rn(v.lo, bitsf(sb));
+#ifdef __CUDA_ARCH__
+    int32_t off = __float2int_rn(scaled);
+#else
+    int32_t off = (int32_t)__builtin_lrintf(scaled);
+#endif
+    int32_t extra = ((hb & 0x007FFFFFu) == 0u) ? (off < 0 ? off : 0) : 0;
+    off += extra;
+    uint64_t bits = ((((uint64_t)Hh) << 32) | Lh) + (uint64_t)(int64_t)off;
+    uint32_t Hr = (uint32_t)(bits >> 32) | (hb & 0x80000000u);
+    uint32_t Lr = (uint32_t)bits;
+    bool tiny = fe < (52u << 23) || (int)(fe >> 23) + ebias <= 0;
+    *H = tiny ? (hb & 0x80000000u) : Hr;
+    *L = tiny ? 0u : Lr;
+}
+
 // split a double constant (host side, exact long-double free): hi = RN_float(x),
 // lo = RN_float(x - hi); |x - (hi+lo)| <= 2^-48 |x|.
 DF_HD f2 split_const(double x) {

@@ -26,6 +26,8 @@ struct Context {
     void* pinned = nullptr;
     size_t pinnedBytes = 0;
     cudaEvent_t pinnedFree = nullptr;
+    // dense gates on 3-4 targets go to the tensor cores (DFS_DENSE_TC=0 disables)
+    bool denseTensorCores = true;
 };
 
 Context& ctx();
@@ -62,6 +64,11 @@ int sv_many_targ(State* s, const unsigned* targs, unsigned k, const double* gate
 int sv_pauli(State* s, const unsigned* targs, const unsigned* paulis, unsigned k, int gadget, double theta);
 int sv_phase_gadget(State* s, const unsigned* targs, unsigned k, double theta);
 int state_scale_real(State* s, double factor);
+
+// k_dense_tc.cu
+bool dense_tc_supported(const State* s, unsigned k);
+int dense_tc(State* s, const unsigned* targs, unsigned k, const double* gate);
+int dense_tc_status();
 
 // k_dm.cu
 int dm_deph1(State* s, unsigned q, double p);

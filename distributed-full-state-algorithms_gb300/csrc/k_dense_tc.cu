@@ -1,0 +1,525 @@
+// k_dense_tc.cu -- manyTargGate (local_statevector_manyTargGate,
+// src/local_statevector.hpp:72-99) on the 5th-generation tensor cores.
+//
+// A dense gate G (D x D complex, D = 2^k) applied to every group of D amplitudes
+// is the real product Y^T = X^T G_R^T: rows are groups (128 per tile, one per
+// thread and TMEM lane), K = N = R = 2D reals ([re(x_0..x_{D-1}), im(...)]).
+// Operands are staged in shared memory in the K-major, unswizzled canonical
+// layout; one thread issues tcgen05.mma; the accumulator lives in TMEM and is
+// read back by tcgen05.ld.
+//
+//  * complex64: 3xTF32.  x = x_big + x_small and g = g_big + g_small in TF32;
+//    D = A_big B_big + A_big B_small + A_small B_big, accumulated in FP32.
+//  * complex128: an exact-integer splitting (Ozaki, Ogita & Oishi, "Error-free
+//    transformation of matrix multiplication by using fast routines of matrix
+//    multiplication and its applications", Numer. Algorithms 59 (2012)).  Every
+//    real of a group is scaled by the group's largest power of two and cut into
+//    six 8-bit integer slices (48 bits), each an exact bf16; every gate row is
+//    cut the same way with its own power of two.  A slice product summed over
+//    K <= 32 terms is an integer below 2^21 and the <= 6 products of equal
+//    weight 2^-8u below 2^24, so the FP32 tensor-core accumulation is exact.
+//    The 21 products with s + t <= 5 go to five TMEM accumulators (the two
+//    lowest weights share one, with B pre-scaled); the epilogue sums them in
+//    double-float (two exact TwoSums, the rest into the error term) and rounds
+//    to the nearest double.
+//    Error: below ~2^-46 of max|x| * max|g| per output (truncated slices and the
+//    dropped products of weight <= 2^-48).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "kernels.cuh"
+#include "tc.cuh"
+
+namespace dfs {
+
+static __device__ int g_tcTimeout;  // set when a bounded MMA wait gave up
+
+constexpr int kTcThreads = 128;
+constexpr int kOzSlices = 6;
+// accumulators: weights 2^0 .. 2^-24 exact (integers below 2^24), and one shared
+// by weights 2^-32 and 2^-40 (the B slices of the latter pre-scaled by 2^-8).  The
+// tensor cores align each product to the accumulator with truncation, so only
+// the two lowest weights may share: their loss (< 96 half-units at 2^-32) stays
+// below 2^-46 of the result, where sharing from 2^-24 down lost ~2^-38.
+constexpr int kOzAccs = 5;
+constexpr int kOzBCopies = 2;
+constexpr uint32_t kTcWaitLimit = 1u << 26;
+
+template <int KT>
+struct Dense {
+    static constexpr int D = 1 << KT;
+    static constexpr int R = 2 * D;             // K = N
+    // bf16 operands (complex128 path)
+    static constexpr uint32_t KG16 = R / 8;     // core matrices along K
+    static constexpr uint32_t A16 = 128 * R * 2;
+    static constexpr uint32_t B16 = R * R * 2;
+    static constexpr uint32_t COLS64 = (kOzAccs * R <= 64) ? 64 : (kOzAccs * R <= 128 ? 128 : 256);
+    static_assert(kOzAccs * R <= 256, "TMEM budget");
+    // tf32 operands (complex64 path)
+    static constexpr uint32_t KG32 = R / 4;
+    static constexpr uint32_t A32 = 128 * R * 4;
+    static constexpr uint32_t B32 = R * R * 4;
+    static constexpr uint32_t COLS32 = R < 32 ? 32 : R;
+};
+
+template <class IT, int KT>
+struct DenseParams {
+    QList q;                  // targets, sorted
+    IT off[1 << KT];          // local index -> amplitude offset (bit i <-> targets[i])
+    int colExp[2 << KT];      // complex128 path: per output real, the power of two of its gate row
+};
+
+// ------------------------------------------------------------ complex128
+
+// double bits -> (sign, 48-bit fraction relative to 2^(E - 1022)) for the group's
+// largest biased exponent E
+DEV uint64_t fraction48(uint32_t H, uint32_t L, uint32_t E) {
+    uint32_t ex = (H >> 20) & 0x7FFu;
+    uint64_t M = ((uint64_t)((H & 0xFFFFFu) | 0x100000u) << 32) | L;
+    uint32_t sh = E - ex + 5u;
+    uint64_t F = sh < 64u ? (M >> sh) : 0ull;
+    return ex == 0u ? 0ull : F;
+}
+
+// sign * b for byte `sel` (0..3) of `word`, as an exact float: the byte is
+// placed under the exponent of the magic +-2^23 (one PRMT), then the magic is
+// subtracted; the float's top 16 bits are the bf16 of the same value
+template <int SEL>
+DEV float float_of_byte(uint32_t word, uint32_t magicBits, float magic) {
+    // result bytes: [magic.b3, magic.b2 (0), magic.b1 (0), word.bSEL]
+    const uint32_t f = __byte_perm(word, magicBits, 0x7650u | SEL);
+    return __fsub_rn(__uint_as_float(f), magic);
+}
+// the bf16 halves of two floats packed as (lo, hi)
+DEV uint32_t pack_bf16(float lo, float hi) { return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632u); }
+
+template <class IT, int KT>
+__global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : 2) k_dense_ozaki(uint4* __restrict__ amps, IT numGroups,
+                                                                DenseParams<IT, KT> p, const uint4* __restrict__ bsl) {
+    using S = Dense<KT>;
+    constexpr int D = S::D, R = S::R, kHalf = D / 2;  // amplitudes per thread
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* sA = smem;
+    unsigned char* sB = smem + kOzSlices * S::A16;  // kOzBCopies x kOzSlices x B16
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmemSlot;
+    __shared__ uint32_t halfMax[2][128];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int row = tid & 127, half = tid >> 7;
+
+    for (int i = tid; i < (int)(kOzBCopies * kOzSlices * S::B16 / 16); i += 2 * kTcThreads)
+        reinterpret_cast<uint4*>(sB)[i] = bsl[i];
+    if (warp == 0) tc::tmem_alloc<S::COLS64>(&tmemSlot);
+    if (tid == 0) tc::mbar_init(&mbar, 1);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tmemSlot;
+    const uint32_t id = tc::idesc(1, R);
+    uint32_t phase = 0;
+    const IT numTiles = (numGroups + 127) / 128;
+
+    // this half's amplitudes of a tile, loaded one tile ahead so that the loads
+    // of tile i+1 are in flight during the MMAs and epilogue of tile i
+    auto load = [&](IT tile, uint4 (&v)[kHalf]) {
+        const IT g = tile * 128 + (IT)row;
+        const bool ok = tile < numTiles && g < numGroups;
+        const IT b = ok ? insert_zeros(g, p.q) : (IT)0;
+#pragma unroll
+        for (int c = 0; c < kHalf; c++) v[c] = ok ? amps[b + p.off[half * kHalf + c]] : make_uint4(0, 0, 0, 0);
+    };
+    uint4 cur[kHalf], nxt[kHalf];
+    load((IT)blockIdx.x, cur);
+
+    for (IT tile = blockIdx.x; tile < numTiles; tile += gridDim.x) {
+        const IT g = tile * 128 + (IT)row;
+        const bool valid = g < numGroups;
+        const IT base = valid ? insert_zeros(g, p.q) : (IT)0;
+
+        // ---- the group's largest exponent (both halves)
+        uint32_t E = 0;
+#pragma unroll
+        for (int c = 0; c < kHalf; c++) E = max(E, max((cur[c].y >> 20) & 0x7FFu, (cur[c].w >> 20) & 0x7FFu));
+        halfMax[half][row] = E;
+        __syncthreads();
+        E = max(E, halfMax[half ^ 1][row]);
+
+        // ---- six 8-bit slices of this half's D reals, 8 reals (one core row) at a time
+#pragma unroll
+        for (int kg = 0; kg < D / 8; kg++) {
+            uint32_t packed[kOzSlices][4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {  // amplitude kg*4 + j: reals (re, im)
+                const uint4 v = cur[kg * 4 + j];
+                float f[2][kOzSlices];
+#pragma unroll
+                for (int part = 0; part < 2; part++) {
+                    const uint32_t H = part ? v.w : v.y, L = part ? v.z : v.x;
+                    uint64_t F = fraction48(H, L, E);
+                    uint32_t Fh = (uint32_t)(F >> 32), Fl = (uint32_t)F;
+                    const bool neg = (H >> 31) != 0u;
+                    const uint32_t mb = neg ? 0xCB000000u : 0x4B000000u;
+                    const float mf = neg ? -8388608.0f : 8388608.0f;
+                    f[part][0] = float_of_byte<1>(Fh, mb, mf);
+                    f[part][1] = float_of_byte<0>(Fh, mb, mf);
+                    f[part][2] = float_of_byte<3>(Fl, mb, mf);
+                    f[part][3] = float_of_byte<2>(Fl, mb, mf);
+                    f[part][4] = float_of_byte<1>(Fl, mb, mf);
+                    f[part][5] = float_of_byte<0>(Fl, mb, mf);
+                }
+#pragma unroll
+                for (int sl = 0; sl < kOzSlices; sl++) packed[sl][j] = pack_bf16(f[0][sl], f[1][sl]);
+            }
+            const uint32_t off = tc::kmajor_offset(row, half * D + kg * 8, S::KG16, 2);
+#pragma unroll
+            for (int sl = 0; sl < kOzSlices; sl++)
+                *reinterpret_cast<uint4*>(sA + sl * S::A16 + off) =
+                    make_uint4(packed[sl][0], packed[sl][1], packed[sl][2], packed[sl][3]);
+        }
+        tc::fence_smem_to_async();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+
+        // ---- the 21 slice products of weight 2^-8u, u = s + t <= 5; u >= 4 share
+        //      accumulator 4 with B pre-scaled by 2^-8(u-4)
+        if (tid == 0) {
+#pragma unroll
+            for (int u = 0; u < kOzSlices; u++) {
+                const int acc = u < kOzAccs ? u : kOzAccs - 1;
+                const int copy = u < kOzAccs ? 0 : u - (kOzAccs - 1);
+#pragma unroll
+                for (int sl = 0; sl <= u; sl++) {
+                    const int t = u - sl;
+#pragma unroll
+                    for (int ks = 0; ks < R / 16; ks++) {
+                        uint64_t da = tc::desc(tc::smem_u32(sA + sl * S::A16 + ks * 256), 128, 128 * S::KG16);
+                        uint64_t db = tc::desc(
+                            tc::smem_u32(sB + (copy * kOzSlices + t) * S::B16 + ks * 256), 128, 128 * S::KG16);
+                        const bool first = u <= kOzAccs - 1 && sl == 0 && ks == 0;
+                        tc::mma_bf16(tmem + (uint32_t)(acc * R), da, db, id, first ? 0u : 1u);
+                    }
+                }
+            }
+            tc::commit(&mbar);
+        }
+        // prefetch the next tile while the tensor cores work
+        load(tile + gridDim.x, nxt);
+
+        const bool ok = tc::mbar_wait(&mbar, phase, kTcWaitLimit);
+        phase ^= 1u;
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicExch(&g_tcTimeout, 1);
+            break;
+        }
+        tc::fence_after_sync();
+
+        // ---- y_n = 2^(E + e_n - 1038) * sum_u D_u[n] 2^(-8u), summed in double-float: D_0,
+        //      D_1 2^-8 and D_2 2^-16 exactly (TwoSum), the rest into the error term
+        float acc[kOzAccs][D];
+        const uint32_t lane = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(half * D);
+#pragma unroll
+        for (int u = 0; u < kOzAccs; u++) {
+            float v[16];
+            if (D >= 16) tc::ld16(lane + (uint32_t)(u * R), v);
+            else tc::ld8(lane + (uint32_t)(u * R), v);
+            tc::ld_wait();
+#pragma unroll
+            for (int j = 0; j < D; j++) acc[u][j] = v[j];
+        }
+        if (valid) {
+#pragma unroll
+            for (int c = 0; c < kHalf; c++) {
+                uint32_t w[4];
+#pragma unroll
+                for (int part = 0; part < 2; part++) {
+                    const int j = 2 * c + part;
+                    df::f2 t = df::two_sum(acc[0][j], acc[1][j] * 0x1p-8f);
+                    df::f2 t2 = df::two_sum(t.hi, acc[2][j] * 0x1p-16f);
+                    float e = df::add_rn(t.lo, t2.lo);
+                    e = __fmaf_rn(acc[3][j], 0x1p-24f, e);
+                    e = __fmaf_rn(acc[4][j], 0x1p-32f, e);
+                    df::f2 y = df::fast_two_sum(t2.hi, e);
+                    // times 2^(E + e_n - 1038), folded into the exponent field
+                    df::encode_words_scaled(y, (int)E + p.colExp[half * D + j] - 1038, &w[2 * part + 1],
+                                            &w[2 * part]);
+                }
+                amps[base + p.off[half * kHalf + c]] = make_uint4(w[0], w[1], w[2], w[3]);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < kHalf; c++) cur[c] = nxt[c];
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_free<S::COLS64>(tmem);
+}
+
+// ------------------------------------------------------------- complex64
+
+DEV uint32_t to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+template <class IT, int KT>
+__global__ void __launch_bounds__(kTcThreads) k_dense_3xtf32(float2* __restrict__ amps, IT numGroups,
+                                                             DenseParams<IT, KT> p, const uint4* __restrict__ bsl) {
+    using S = Dense<KT>;
+    constexpr int D = S::D, R = S::R;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* sAbig = smem;
+    unsigned char* sAsmall = smem + S::A32;
+    unsigned char* sB = smem + 2 * S::A32;  // big then small
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmemSlot;
+    const int tid = threadIdx.x, warp = tid >> 5;
+
+    for (int i = tid; i < (int)(2 * S::B32 / 16); i += kTcThreads) reinterpret_cast<uint4*>(sB)[i] = bsl[i];
+    if (warp == 0) tc::tmem_alloc<S::COLS32>(&tmemSlot);
+    if (tid == 0) tc::mbar_init(&mbar, 1);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tmemSlot;
+    const uint32_t id = tc::idesc(2, R);
+    uint32_t phase = 0;
+    const IT numTiles = (numGroups + 127) / 128;
+
+    for (IT tile = blockIdx.x; tile < numTiles; tile += gridDim.x) {
+        const IT g = tile * 128 + (IT)tid;
+        const bool valid = g < numGroups;
+        const IT base = valid ? insert_zeros(g, p.q) : (IT)0;
+        float x[R];  // reals ordered [re x0, im x0, re x1, ...]
+#pragma unroll
+        for (int c = 0; c < D; c++) {
+            float2 v = valid ? amps[base + p.off[c]] : make_float2(0.f, 0.f);
+            x[2 * c] = v.x;
+            x[2 * c + 1] = v.y;
+        }
+#pragma unroll
+        for (int kg = 0; kg < R / 4; kg++) {
+            uint32_t big[4], small[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                float v = x[kg * 4 + j];
+                big[j] = to_tf32(v);
+                small[j] = to_tf32(__fsub_rn(v, __uint_as_float(big[j])));
+            }
+            const uint32_t off = tc::kmajor_offset(tid, kg * 4, S::KG32, 4);
+            *reinterpret_cast<uint4*>(sAbig + off) = make_uint4(big[0], big[1], big[2], big[3]);
+            *reinterpret_cast<uint4*>(sAsmall + off) = make_uint4(small[0], small[1], small[2], small[3]);
+        }
+        tc::fence_smem_to_async();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (tid == 0) {
+            const uint32_t lbo = 128, sbo = 128 * S::KG32;
+#pragma unroll
+            for (int ks = 0; ks < R / 8; ks++) {
+                uint64_t ab = tc::desc(tc::smem_u32(sAbig + ks * 256), lbo, sbo);
+                uint64_t as = tc::desc(tc::smem_u32(sAsmall + ks * 256), lbo, sbo);
+                uint64_t bb = tc::desc(tc::smem_u32(sB + ks * 256), lbo, sbo);
+                uint64_t bs = tc::desc(tc::smem_u32(sB + S::B32 + ks * 256), lbo, sbo);
+                tc::mma_tf32(tmem, as, bb, id, ks > 0 ? 1u : 0u);
+                tc::mma_tf32(tmem, ab, bs, id, 1u);
+                tc::mma_tf32(tmem, ab, bb, id, 1u);
+            }
+            tc::commit(&mbar);
+        }
+        const bool ok = tc::mbar_wait(&mbar, phase, kTcWaitLimit);
+        phase ^= 1u;
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicExch(&g_tcTimeout, 1);
+            break;
+        }
+        tc::fence_after_sync();
+        float y[R];
+        const uint32_t lane = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+        for (int nc = 0; nc < R / 16; nc++) {
+            float v[16];
+            tc::ld16(lane + (uint32_t)(nc * 16), v);
+            tc::ld_wait();
+#pragma unroll
+            for (int j = 0; j < 16; j++) y[nc * 16 + j] = v[j];
+        }
+        if (valid) {
+#pragma unroll
+            for (int c = 0; c < D; c++) amps[base + p.off[c]] = make_float2(y[2 * c], y[2 * c + 1]);
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_free<S::COLS32>(tmem);
+}
+
+// ------------------------------------------------------------------ host
+
+// G_R[n][kk], reals ordered [re x0, im x0, re x1, ...]: output real n = 2r + pn
+// (pn = 0 real part) from input real kk = 2c + pk
+static double real_form(const double* g, int D, int n, int kk) {
+    int r = n / 2, c = kk / 2, pn = n & 1, pk = kk & 1;
+    double re = g[2 * (r * D + c)], im = g[2 * (r * D + c) + 1];
+    if (pn == 0) return pk == 0 ? re : -im;
+    return pk == 0 ? im : re;
+}
+
+template <int KT>
+static void prepare_ozaki_b(const double* g, std::vector<unsigned char>& bytes, int* colExp) {
+    using S = Dense<KT>;
+    constexpr int D = S::D, R = S::R;
+    bytes.assign(kOzBCopies * kOzSlices * S::B16, 0);
+    for (int n = 0; n < R; n++) {
+        int F = 0;
+        bool any = false;
+        for (int kk = 0; kk < R; kk++) {
+            double v = real_form(g, D, n, kk);
+            if (v != 0.0) {
+                int e;
+                std::frexp(v, &e);
+                F = any ? std::max(F, e) : e;
+                any = true;
+            }
+        }
+        colExp[n] = F;
+        for (int kk = 0; kk < R; kk++) {
+            double v = real_form(g, D, n, kk);
+            double scaled = std::ldexp(std::fabs(v), 48 - F);  // < 2^48, exact
+            uint64_t V = (uint64_t)scaled;                     // floor
+            uint16_t sign = v < 0 ? 0x8000 : 0;
+            for (int copy = 0; copy < kOzBCopies; copy++)
+                for (int t = 0; t < kOzSlices; t++) {
+                    uint32_t byte = (uint32_t)((V >> (8 * (kOzSlices - 1 - t))) & 0xFF);
+                    float f = std::ldexp((float)byte, -8 * copy);  // exact power-of-two scaling
+                    uint32_t fb;
+                    std::memcpy(&fb, &f, 4);
+                    uint16_t h = (uint16_t)(fb >> 16) | (byte ? sign : 0);
+                    uint32_t off = (copy * kOzSlices + t) * S::B16 + tc::kmajor_offset(n, kk, S::KG16, 2);
+                    std::memcpy(&bytes[off], &h, 2);
+                }
+        }
+    }
+}
+
+static uint32_t host_tf32(float x) {
+    uint32_t b;
+    std::memcpy(&b, &x, 4);
+    // round to nearest, ties away from zero, on the 13 dropped bits
+    uint32_t r = (b + 0x1000u) & 0xFFFFE000u;
+    return r;
+}
+
+template <int KT>
+static void prepare_tf32_b(const double* g, std::vector<unsigned char>& bytes) {
+    using S = Dense<KT>;
+    constexpr int D = S::D, R = S::R;
+    bytes.assign(2 * S::B32, 0);
+    for (int n = 0; n < R; n++)
+        for (int kk = 0; kk < R; kk++) {
+            float v = (float)real_form(g, D, n, kk);
+            uint32_t big = host_tf32(v);
+            float bigf;
+            std::memcpy(&bigf, &big, 4);
+            uint32_t small = host_tf32(v - bigf);
+            uint32_t off = tc::kmajor_offset(n, kk, S::KG32, 4);
+            std::memcpy(&bytes[off], &big, 4);
+            std::memcpy(&bytes[S::B32 + off], &small, 4);
+        }
+}
+
+template <class IT, int KT>
+static DenseParams<IT, KT> dense_params(const unsigned* targs) {
+    DenseParams<IT, KT> p{};
+    p.q = make_qlist(std::vector<unsigned>(targs, targs + KT));
+    for (int c = 0; c < (1 << KT); c++) {
+        uint64_t o = 0;
+        for (int b = 0; b < KT; b++) o |= (uint64_t)((c >> b) & 1) << targs[b];
+        p.off[c] = (IT)o;
+    }
+    return p;
+}
+
+// dynamic shared memory for the launch, and the whole unified L1/shared array as
+// shared memory (the default carve-out leaves room for only one of these CTAs)
+template <class K>
+static int set_smem(K kernel, size_t bytes) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    return e == cudaSuccess ? DFS_SUCCESS : cuda_fail(e, "cudaFuncSetAttribute(dense)");
+}
+
+template <class IT, int KT>
+static int dense_tc_run(State* s, const unsigned* targs, const double* g) {
+    using S = Dense<KT>;
+    const IT groups = (IT)(s->numAmps >> KT);
+    const uint64_t tiles = (groups + 127) / 128;
+    DenseParams<IT, KT> p = dense_params<IT, KT>(targs);
+    std::vector<unsigned char> bytes;
+    size_t smem;
+    int ctasPerSM;
+    if (s->precision == DFS_C64) {
+        prepare_tf32_b<KT>(g, bytes);
+        smem = 2 * S::A32 + 2 * S::B32;
+        ctasPerSM = (int)std::min<uint32_t>(4, 512 / S::COLS32);
+    } else {
+        prepare_ozaki_b<KT>(g, bytes, p.colExp);
+        smem = kOzSlices * S::A16 + kOzBCopies * kOzSlices * S::B16;
+        ctasPerSM = (int)(512 / S::COLS64);
+    }
+    // at most ctasPerSM CTAs may share an SM's 512 TMEM columns: pad the dynamic shared
+    // memory so that ctasPerSM + 1 cannot be resident (each also holds <= 2 KiB static
+    // + 1 KiB reserved)
+    const size_t perSM = ctx().smemOptin + 1024, reserve = 3 * 1024;
+    size_t minSmem = perSM / (size_t)(ctasPerSM + 1) + 1;
+    size_t maxSmem = perSM / (size_t)ctasPerSM - reserve;
+    if (smem < minSmem) smem = std::min(minSmem, maxSmem);
+    int rc = upload_scratch(bytes.data(), bytes.size(), 0);
+    if (rc) return rc;
+    // persistent grid of ctasPerSM CTAs per SM (the padding above keeps any more from
+    // sharing an SM's TMEM; if fewer fit at once, the rest run as a second wave)
+    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(tiles, (uint64_t)ctx().numSMs * ctasPerSM));
+    if (s->precision == DFS_C64) {
+        auto kern = k_dense_3xtf32<IT, KT>;
+        if ((rc = set_smem(kern, smem))) return rc;
+        kern<<<grid, kTcThreads, smem, ctx().stream>>>((float2*)s->amps, groups, p, (const uint4*)ctx().scratch);
+    } else {
+        auto kern = k_dense_ozaki<IT, KT>;
+        if ((rc = set_smem(kern, smem))) return rc;
+        kern<<<grid, 2 * kTcThreads, smem, ctx().stream>>>((uint4*)s->amps, groups, p, (const uint4*)ctx().scratch);
+    }
+    return check_launch("manyTargGate (tensor cores)");
+}
+
+// measured at 30 qubits: complex128 k=3 3.4 TB/s (CUDA cores 2.4), k=4 3.2 (0.75);
+// complex64 k=4 5.2 TB/s (0.9), while k=3 stays on the FP32 CUDA cores (6.0 vs 4.9)
+bool dense_tc_supported(const State* s, unsigned k) {
+    if (s->precision == DFS_C128_NATIVE || !ctx().denseTensorCores) return false;
+    if (s->precision == DFS_C64) return k == 4;
+    return k == 3 || k == 4;
+}
+
+int dense_tc(State* s, const unsigned* targs, unsigned k, const double* gate) {
+    bool wide = s->numAmps > (1ull << 31);
+    switch (k) {
+        case 3: return wide ? dense_tc_run<uint64_t, 3>(s, targs, gate) : dense_tc_run<uint32_t, 3>(s, targs, gate);
+        case 4: return wide ? dense_tc_run<uint64_t, 4>(s, targs, gate) : dense_tc_run<uint32_t, 4>(s, targs, gate);
+        default: return fail(DFS_ERR_INVALID_ARG, "no tensor-core path for %u targets", k);
+    }
+}
+
+int dense_tc_status() {
+    int v = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_tcTimeout, sizeof(int));
+    if (e != cudaSuccess) return cuda_fail(e, "tensor-core status");
+    return v ? fail(DFS_ERR_TIMEOUT, "a tensor-core kernel gave up waiting for its MMAs") : DFS_SUCCESS;
+}
+
+}  // namespace dfs

@@ -388,6 +388,7 @@ static int many_targ_reg(State* s, const unsigned* targs, const double* g) {
 struct RunManyTarg {
     template <class P, class IT>
     static int run(State* s, const unsigned* targs, unsigned k, const double* g) {
+        if (dense_tc_supported(s, k)) return dense_tc(s, targs, k, g);
         switch (k) {
             case 1: return many_targ_reg<P, IT, 1>(s, targs, g);
             case 2: return many_targ_reg<P, IT, 2>(s, targs, g);

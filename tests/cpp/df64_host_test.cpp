@@ -75,8 +75,23 @@ int main() {
         double err = (double)(std::fabs((double)((__float128)from_words(H, L) - ex)) / mag);
         if (err > worstDot) worstDot = err;
     }
-    printf("decode %.3e encode %.3e dot4 %.3e zero %ld\n", worstDec, worstEnc, worstDot, zeroFail);
+    // encode_words_scaled == encode_words times 2^shift
+    long scaledBad = 0;
+    for (long it = 0; it < 200000; it++) {
+        float hi = (float)(nd(rng) * std::pow(2.0, ue(rng) / 4));
+        float ulp = std::nextafter(std::fabs(hi), INFINITY) - std::fabs(hi);
+        float lo = (float)(std::uniform_real_distribution<double>(-0.5, 0.5)(rng) * ulp);
+        f2 q = fast_two_sum(hi, lo);
+        int shift = (int)(ue(rng) * 8);  // -576 .. 320
+        uint32_t H, L, H2, L2;
+        encode_words(q, &H, &L);
+        encode_words_scaled(q, shift, &H2, &L2);
+        double want = std::ldexp(from_words(H, L), shift);
+        if (std::fabs(want) < 0x1p-1020) want = 0.0;  // flushed below the normal range
+        if (from_words(H2, L2) != want) scaledBad++;
+    }
+    printf("decode %.3e encode %.3e dot4 %.3e zero %ld scaled %ld\n", worstDec, worstEnc, worstDot, zeroFail, scaledBad);
     bool ok = worstDec <= std::ldexp(1.0, -47) && worstEnc <= std::ldexp(1.0, -52) && worstDot <= std::ldexp(1.0, -44) &&
-              zeroFail == 0;
+              zeroFail == 0 && scaledBad == 0;
     return ok ? 0 : 1;
 }

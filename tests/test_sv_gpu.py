@@ -189,3 +189,33 @@ def test_reductions_sv(dfs, oracle, rng):
         b = phi.getAllVecAmps()
         ip = dfs.inner_product(psi, phi)
         assert abs(ip - np.vdot(a, b)) <= tol * np.linalg.norm(a) * np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+@pytest.mark.parametrize("k", [3, 4])
+def test_dense_gate_extreme_magnitudes(dfs, oracle, prec, k, rng):
+    """The tensor-core dense path scales each group by its largest power of two:
+    groups mixing 1e-30 and 1, exact zeros, negative zeros and whole zero groups
+    must still come out within tolerance of the largest amplitude."""
+    n = 11
+    N = 1 << n
+    a = gaussian_state(rng, N)
+    a[::7] *= 1e-30
+    a[::11] = 0.0
+    a[3::13] = -0.0
+    a[: N // 8] = 0.0                     # whole groups of zeros
+    a[N // 2::5] *= 1e12
+    targs = [int(q) for q in rng.permutation(n)[:k]]
+    g = gaussian_matrix(rng, 1 << k)
+    g[0, :] *= 1e-9                       # gate rows of very different scale
+    psi = dfs.StateVector(n, precision=prec)
+    psi.setAmps(a)
+    if prec == "c64":
+        a = psi.getAllVecAmps()
+    dfs.distributed_statevector_manyTargGate(psi, targs, g)
+    oracle.sv_many_targ(a, targs, g)
+    got = psi.getAllVecAmps()
+    assert np.all(np.isfinite(got))
+    assert rel_err(got, a) <= TOL[prec]
+    zero_groups = np.abs(a) == 0
+    assert np.all(got[zero_groups] == 0)
