@@ -110,6 +110,25 @@ PROTOTYPES = {
     "dfs_state_norm_squared": [_H, _DP],
     "dfs_densitymatrix_trace": [_H, _DP, _DP],
     "dfs_densitymatrix_expecPauliString_noalloc": [_H, _DP, _U, _UP, _DP, _DP],
+    "dfs_circuit_create": [_U, _I, _HP],
+    "dfs_circuit_destroy": [_H],
+    "dfs_circuit_num_params": [_H, _UP],
+    "dfs_circuit_num_ops": [_H, _UP],
+    "dfs_circuit_oneTargGate": [_H, _U, _DP],
+    "dfs_circuit_manyCtrlOneTargGate": [_H, _UP, _U, _U, _DP],
+    "dfs_circuit_swapGate": [_H, _U, _U],
+    "dfs_circuit_manyTargGate": [_H, _UP, _U, _DP],
+    "dfs_circuit_pauliTensor": [_H, _UP, _UP, _U],
+    "dfs_circuit_pauliGadget": [_H, _UP, _UP, _U, _I, _D],
+    "dfs_circuit_phaseGadget": [_H, _UP, _U, _I, _D],
+    "dfs_circuit_oneQubitDephasing": [_H, _U, _I, _D],
+    "dfs_circuit_twoQubitDephasing": [_H, _U, _U, _I, _D],
+    "dfs_circuit_oneQubitDepolarising": [_H, _U, _I, _D],
+    "dfs_circuit_twoQubitDepolarising": [_H, _U, _U, _I, _D],
+    "dfs_circuit_damping": [_H, _U, _I, _D],
+    "dfs_circuit_apply": [_H, _H, _DP],
+    "dfs_circuit_expec": [_H, _H, _DP, _DP, _U, _UP, _DP],
+    "dfs_circuit_gradient": [_H, _DP, _DP],
     "dfs_error_string": [_I],
     "dfs_last_error": [],
 }

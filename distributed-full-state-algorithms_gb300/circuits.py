@@ -124,9 +124,82 @@ def gadget_ansatz(num_qubits: int, layers: int, per_layer: int, seed: int) -> li
     rng = np.random.default_rng(seed)
     gates = []
     for _ in range(layers * per_layer):
-        t, p = random_pauli_string(rng, num_qubits, int(rng.integers(2, 5)))
+        t, p = random_pauli_string(rng, num_qubits, int(rng.integers(2, min(4, num_qubits) + 1)))
         gates.append(Gate("pauli_gadget", t, paulis=p, param=float(rng.normal())))
     return gates
+
+
+def dm_gadget_ansatz(num_qubits: int, layers: int, per_layer: int, seed: int, max_prob: float = 0.05) -> list[Gate]:
+    """Density-matrix ansatz: per layer, ``per_layer`` Pauli gadgets (theta ~ N(0,1)) then
+    one-qubit depolarising and damping on random qubits with prob ~ U[0, max_prob]."""
+    rng = np.random.default_rng(seed)
+    gates = []
+    for _ in range(layers):
+        for _ in range(per_layer):
+            t, p = random_pauli_string(rng, num_qubits, int(rng.integers(2, min(4, num_qubits) + 1)))
+            gates.append(Gate("pauli_gadget", t, paulis=p, param=float(rng.normal())))
+        gates.append(Gate("depol1", (int(rng.integers(num_qubits)),), param=float(rng.uniform(0, max_prob))))
+        gates.append(Gate("damping", (int(rng.integers(num_qubits)),), param=float(rng.uniform(0, max_prob))))
+    return gates
+
+
+PARAM_KINDS = ("pauli_gadget", "phase_gadget", "deph1", "deph2", "depol1", "depol2", "damping")
+
+
+def record(dfs, num_qubits: int, gates: Sequence[Gate], density_matrix: bool = False,
+           parametrise: Sequence[str] = PARAM_KINDS):
+    """Record ``gates`` into an engine ``Circuit``; the angle or probability of every gate
+    whose kind is in ``parametrise`` becomes the next parameter.  Returns (circuit, params)."""
+    c = dfs.Circuit(num_qubits, densityMatrix=density_matrix)
+    params = []
+
+    def slot(g):
+        if g.kind in parametrise:
+            params.append(g.param)
+            return {"param": len(params) - 1}
+        return {}
+
+    for g in gates:
+        k = g.kind
+        if k == "one_targ":
+            c.oneTargGate(g.qubits[0], g.matrix)
+        elif k == "ctrl":
+            c.manyCtrlOneTargGate(g.controls, g.qubits[0], g.matrix)
+        elif k == "swap":
+            c.swapGate(g.qubits[0], g.qubits[1])
+        elif k in ("many_targ", "dm_many_targ"):
+            c.manyTargGate(g.qubits, g.matrix)
+        elif k == "pauli_tensor":
+            c.pauliTensor(g.qubits, g.paulis)
+        elif k == "pauli_gadget":
+            c.pauliGadget(g.qubits, g.paulis, g.param, **slot(g))
+        elif k == "phase_gadget":
+            c.phaseGadget(g.qubits, g.param, **slot(g))
+        elif k == "deph1":
+            c.oneQubitDephasing(g.qubits[0], g.param, **slot(g))
+        elif k == "deph2":
+            c.twoQubitDephasing(g.qubits[0], g.qubits[1], g.param, **slot(g))
+        elif k == "depol1":
+            c.oneQubitDepolarising(g.qubits[0], g.param, **slot(g))
+        elif k == "depol2":
+            c.twoQubitDepolarising(g.qubits[0], g.qubits[1], g.param, **slot(g))
+        elif k == "damping":
+            c.damping(g.qubits[0], g.param, **slot(g))
+        else:
+            raise ValueError(f"unknown gate kind {k}")
+    return c, np.asarray(params, dtype=np.float64)
+
+
+def with_params(gates: Sequence[Gate], params, parametrise: Sequence[str] = PARAM_KINDS) -> list[Gate]:
+    """A copy of ``gates`` whose parametrised angles/probabilities are taken from ``params``
+    in order (the numbering ``record`` uses)."""
+    out, i = [], 0
+    for g in gates:
+        if g.kind in parametrise:
+            g = Gate(g.kind, g.qubits, g.controls, g.matrix, g.paulis, float(params[i]))
+            i += 1
+        out.append(g)
+    return out
 
 
 # ------------------------------------------------------------- application
@@ -165,12 +238,41 @@ def apply(dfs, state, gates: Sequence[Gate]) -> None:
             raise ValueError(f"unknown gate kind {k}")
 
 
-def apply_to(backend, amps: np.ndarray, gates: Sequence[Gate]) -> None:
+def controlled(matrix: np.ndarray, num_controls: int) -> np.ndarray:
+    """The dense matrix of a gate with controls, on targets (target, controls...):
+    local index bit 0 addresses the target; identity unless every control bit is 1."""
+    d = 1 << (num_controls + 1)
+    u = np.eye(d, dtype=np.complex128)
+    u[d - 2:, d - 2:] = matrix
+    return u
+
+
+_DM_EQUIVALENT = {"one_targ": "dm_many_targ", "many_targ": "dm_many_targ", "swap": "dm_swap",
+                  "pauli_gadget": "dm_pauli_gadget", "phase_gadget": "dm_phase_gadget",
+                  "pauli_tensor": "dm_pauli_tensor"}
+
+
+def apply_to(backend, amps: np.ndarray, gates: Sequence[Gate], dm: bool = False) -> None:
     """Run a circuit through an object with the oracle's method names
-    (``sv_one_targ(amps, ...)`` etc.), e.g. the parity checker."""
+    (``sv_one_targ(amps, ...)`` etc.), e.g. the parity checker.  With ``dm`` the
+    unitary kinds act on a density matrix (U on the ket qubits, conj(U) on the bra
+    qubits); a controlled gate becomes the dense controlled unitary."""
     for g in gates:
         k = g.kind
-        if k == "one_targ":
+        if dm and k == "ctrl":
+            backend.dm_many_targ(amps, (g.qubits[0],) + tuple(g.controls), controlled(g.matrix, len(g.controls)))
+            continue
+        if dm:
+            k = _DM_EQUIVALENT.get(k, k)
+        if k == "dm_swap":
+            backend.dm_swap(amps, g.qubits[0], g.qubits[1])
+        elif k == "dm_pauli_gadget":
+            backend.dm_pauli_gadget(amps, g.qubits, g.paulis, g.param)
+        elif k == "dm_phase_gadget":
+            backend.dm_phase_gadget(amps, g.qubits, g.param)
+        elif k == "dm_pauli_tensor":
+            backend.dm_pauli_tensor(amps, g.qubits, g.paulis)
+        elif k == "one_targ":
             backend.sv_one_targ(amps, g.qubits[0], g.matrix)
         elif k == "ctrl":
             backend.sv_many_ctrl_one_targ(amps, g.controls, g.qubits[0], g.matrix)

@@ -1,0 +1,745 @@
+// circuit.cu -- the circuit runtime: recorded operation sequences, forward runs,
+// and the adjoint-state gradient of <H> (no reference counterpart; each recorded
+// operation is one of the reference's distributed_statevector_* /
+// distributed_densitymatrix_* functions, src/distributed_statevector.hpp:18-298,
+// src/distributed_densitymatrix.hpp:15-319).
+//
+// Backward sweep, for operations i = L..1 with the state psi_i and the adjoint
+// lam_i (= H psi_L, or vec H, at i = L):
+//   parametrised gadget exp(i phi Q):  dL/dphi = -2 Im <lam_i|Q|psi_i> (statevector) or
+//                                      -Im <lam_i, Q rho_i> (density matrix, linear loss),
+//                                      then both <- exp(-i phi Q) in the same kernel;
+//   other unitaries:                   both <- U^dagger;
+//   channels / non-unitary matrices:   rho_{i-1} <- checkpoint taken in the forward pass,
+//                                      dL/dp = Re <lam_i, (dS/dp) rho_{i-1}>, lam <- S^dagger lam.
+// A density-matrix gadget is two gadgets on the vectorised state (ket targets with
+// angle theta, bra targets with -theta, or +theta for an odd number of Y), undone
+// bra first, each contributing with the sign of its angle.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <vector>
+
+#include "adjoint.hpp"
+
+namespace dfs {
+
+enum OpKind {
+    OP_ONE_TARG,
+    OP_CTRL,
+    OP_SWAP,
+    OP_MANY_TARG,
+    OP_PAULI_TENSOR,
+    OP_PAULI_GADGET,
+    OP_PHASE_GADGET,
+    OP_DEPH1,
+    OP_DEPH2,
+    OP_DEPOL1,
+    OP_DEPOL2,
+    OP_DAMPING,
+};
+
+struct CircOp {
+    OpKind kind;
+    std::vector<unsigned> targs, ctrls, paulis;
+    std::vector<double> gate, gateAdj;  // interleaved row-major, and its conjugate transpose
+    bool invertible = true;             // false: the forward pass keeps a checkpoint
+    int param = -1;
+    double value = 0;
+    double val(const double* params) const { return param >= 0 ? params[param] : value; }
+    bool is_channel() const { return kind >= OP_DEPH1; }
+};
+
+struct Circuit {
+    unsigned numQubits = 0;
+    int isDM = 0;
+    std::vector<CircOp> ops;
+    int numParams = 0;
+    // working storage, allocated on first use
+    State* work = nullptr;
+    State* adj = nullptr;
+    std::vector<State*> ckpt;  // one per non-invertible operation, in order
+    void* dev = nullptr;       // terms | partial rows | row sums
+    size_t devBytes = 0;
+    // the latest forward pass
+    bool haveForward = false;
+    std::vector<double> fwdParams;
+    std::vector<AdjTerm> terms;
+    std::vector<double> coeffs;
+    std::vector<unsigned> paulis;
+};
+
+}  // namespace dfs
+
+struct dfs_circuit_s : dfs::Circuit {};
+
+namespace dfs {
+
+// ------------------------------------------------------------- helpers
+
+static int check_q(const Circuit* c, unsigned q) {
+    return q < c->numQubits ? DFS_SUCCESS : fail(DFS_ERR_QUBIT_INDEX, "qubit %u out of range [0, %u)", q, c->numQubits);
+}
+
+static int check_qs(const Circuit* c, const unsigned* qs, unsigned num, bool allowEmpty) {
+    if (num == 0) return allowEmpty ? DFS_SUCCESS : fail(DFS_ERR_INVALID_ARG, "empty qubit list");
+    if (!qs) return fail(DFS_ERR_INVALID_ARG, "null qubit list");
+    if (num > (unsigned)kMaxList) return fail(DFS_ERR_TOO_LARGE, "too many qubits (%u)", num);
+    uint64_t seen = 0;
+    for (unsigned i = 0; i < num; i++) {
+        int rc = check_q(c, qs[i]);
+        if (rc) return rc;
+        if (seen >> qs[i] & 1) return fail(DFS_ERR_DUPLICATE_QUBIT, "qubit %u repeated", qs[i]);
+        seen |= 1ull << qs[i];
+    }
+    return DFS_SUCCESS;
+}
+
+static int check_param(int param, double value, bool isProb) {
+    if (param >= 1 << 24) return fail(DFS_ERR_INVALID_ARG, "parameter index %d too large", param);
+    if (param < 0 && isProb && !(value >= 0.0 && value <= 1.0))
+        return fail(DFS_ERR_INVALID_ARG, "probability %g outside [0, 1]", value);
+    return DFS_SUCCESS;
+}
+
+static void note_param(Circuit* c, int param) {
+    if (param >= 0) c->numParams = std::max(c->numParams, param + 1);
+}
+
+static void set_gate(CircOp& op, const double* g, size_t dim) {
+    op.gate.assign(g, g + 2 * dim * dim);
+    op.gateAdj.assign(2 * dim * dim, 0.0);
+    double dev = 0;
+    for (size_t r = 0; r < dim; r++)
+        for (size_t c = 0; c < dim; c++) {
+            op.gateAdj[2 * (c * dim + r)] = g[2 * (r * dim + c)];
+            op.gateAdj[2 * (c * dim + r) + 1] = -g[2 * (r * dim + c) + 1];
+        }
+    // unitarity: max |(U^dagger U - I)_{rc}|
+    for (size_t r = 0; r < dim; r++)
+        for (size_t c = 0; c < dim; c++) {
+            std::complex<double> s = 0;
+            for (size_t k = 0; k < dim; k++)
+                s += std::conj(std::complex<double>(g[2 * (k * dim + r)], g[2 * (k * dim + r) + 1])) *
+                     std::complex<double>(g[2 * (k * dim + c)], g[2 * (k * dim + c) + 1]);
+            if (r == c) s -= 1.0;
+            dev = std::max(dev, std::abs(s));
+        }
+    op.invertible = dev <= 1e-12 * (double)dim;
+}
+
+static void pauli_masks(const std::vector<unsigned>& targs, const std::vector<unsigned>& paulis, unsigned shift,
+                        uint64_t* mX, uint64_t* mYZ, int* numY) {
+    *mX = 0;
+    *mYZ = 0;
+    *numY = 0;
+    for (size_t i = 0; i < targs.size(); i++) {
+        unsigned p = paulis[i], q = targs[i] + shift;
+        if (p == 1 || p == 2) *mX |= 1ull << q;
+        if (p == 2 || p == 3) *mYZ |= 1ull << q;
+        if (p == 2) (*numY)++;
+    }
+}
+
+static bool odd_y(const std::vector<unsigned>& paulis) {
+    int c = 0;
+    for (unsigned p : paulis) c += p == 2;
+    return c & 1;
+}
+
+// ------------------------------------------------------- operation replay
+
+// forward (adjoint = false) or adjoint (adjoint = true: U^dagger, -theta) of a
+// unitary operation; channels go forward only
+static int apply_op(State* s, const CircOp& op, double v, bool adjoint) {
+    const double* g = adjoint ? op.gateAdj.data() : op.gate.data();
+    const unsigned k = (unsigned)op.targs.size();
+    const unsigned* t = op.targs.data();
+    const double th = adjoint ? -v : v;
+    if (!s->isDM) {
+        switch (op.kind) {
+            case OP_ONE_TARG: return sv_one_targ(s, t[0], g);
+            case OP_CTRL: return sv_ctrl_one_targ(s, op.ctrls.data(), (unsigned)op.ctrls.size(), t[0], g);
+            case OP_SWAP: return sv_swap(s, t[0], t[1]);
+            case OP_MANY_TARG: return sv_many_targ(s, t, k, g);
+            case OP_PAULI_TENSOR: return sv_pauli(s, t, op.paulis.data(), k, 0, 0.0);
+            case OP_PAULI_GADGET: return sv_pauli(s, t, op.paulis.data(), k, 1, th);
+            case OP_PHASE_GADGET: return sv_phase_gadget(s, t, k, th);
+            default: return fail(DFS_ERR_STATE_KIND, "channel in a statevector circuit");
+        }
+    }
+    dfs_state d = static_cast<dfs_state>(s);
+    switch (op.kind) {
+        case OP_ONE_TARG:
+        case OP_MANY_TARG: return dfs_densitymatrix_manyTargGate(d, t, k, g);
+        case OP_CTRL: {
+            // the density-matrix form of a controlled gate: controls and target on the
+            // ket qubits with U, and on the bra qubits with conj(U)
+            int rc = sv_ctrl_one_targ(s, op.ctrls.data(), (unsigned)op.ctrls.size(), t[0], g);
+            if (rc) return rc;
+            std::vector<unsigned> cb(op.ctrls);
+            for (unsigned& q : cb) q += s->numQubits;
+            std::vector<double> conjG(g, g + 8);
+            for (int e = 0; e < 4; e++) conjG[2 * e + 1] = -conjG[2 * e + 1];
+            return sv_ctrl_one_targ(s, cb.data(), (unsigned)cb.size(), t[0] + s->numQubits, conjG.data());
+        }
+        case OP_SWAP: return dfs_densitymatrix_swapGate(d, t[0], t[1]);
+        case OP_PAULI_TENSOR: return dfs_densitymatrix_pauliTensor(d, t, op.paulis.data(), k);
+        case OP_PAULI_GADGET: return dfs_densitymatrix_pauliGadget(d, t, op.paulis.data(), k, th);
+        case OP_PHASE_GADGET: return dfs_densitymatrix_phaseGadget(d, t, k, th);
+        case OP_DEPH1: return dm_deph1(s, t[0], v);
+        case OP_DEPH2: return dm_deph2(s, t[0], t[1], v);
+        case OP_DEPOL1: return dm_depol1(s, t[0], v);
+        case OP_DEPOL2: return dm_depol2(s, t[0], t[1], v, 0);
+        case OP_DAMPING: return dm_damping(s, t[0], v);
+    }
+    return fail(DFS_ERR_INVALID_ARG, "unknown operation");
+}
+
+// --------------------------------------------------- channel superoperators
+// Forward maths of the channel kernels (src/local_densitymatrix.hpp:12-131 and the
+// constants of src/distributed_densitymatrix.hpp:92-319) as matrices S(p), with
+// their derivatives, on the group elements e = ket bits | bra bits << K.
+
+static void channel_mats1(const CircOp& op, unsigned n, double p, ChannelMats<1>* m) {
+    double S[4][4] = {}, D[4][4] = {};
+    switch (op.kind) {
+        case OP_DEPH1:
+            S[0][0] = S[3][3] = 1;
+            S[1][1] = S[2][2] = 1 - 2 * p;
+            D[1][1] = D[2][2] = -2;
+            break;
+        case OP_DEPOL1:
+            S[0][0] = S[3][3] = 1 - 2 * p / 3;
+            S[0][3] = S[3][0] = 2 * p / 3;
+            S[1][1] = S[2][2] = 1 - 4 * p / 3;
+            D[0][0] = D[3][3] = -2.0 / 3;
+            D[0][3] = D[3][0] = 2.0 / 3;
+            D[1][1] = D[2][2] = -4.0 / 3;
+            break;
+        default:  // damping
+            S[0][0] = 1;
+            S[0][3] = p;
+            S[1][1] = S[2][2] = std::sqrt(1 - p);
+            S[3][3] = 1 - p;
+            D[0][3] = 1;
+            D[1][1] = D[2][2] = p < 1 ? -0.5 / std::sqrt(1 - p) : 0.0;
+            D[3][3] = -1;
+            break;
+    }
+    m->bits[0] = (int)op.targs[0];
+    m->bits[1] = (int)(op.targs[0] + n);
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++) {
+            m->st[r][c] = S[c][r];
+            m->d[r][c] = D[r][c];
+        }
+}
+
+static void channel_mats2(const CircOp& op, unsigned n, double p, ChannelMats<2>* m) {
+    double S[16][16] = {}, D[16][16] = {};
+    auto diag = [](int e) { return (e & 3) == (e >> 2); };  // ket bits == bra bits
+    for (int e = 0; e < 16; e++) {
+        if (op.kind == OP_DEPH2) {
+            S[e][e] = diag(e) ? 1 : 1 - 4 * p / 3;
+            D[e][e] = diag(e) ? 0 : -4.0 / 3;
+            continue;
+        }
+        // trace-preserving two-qubit depolarising
+        if (!diag(e)) {
+            S[e][e] = 1 - 16 * p / 15;
+            D[e][e] = -16.0 / 15;
+            continue;
+        }
+        for (int f = 0; f < 16; f++) {
+            if (!diag(f)) continue;
+            S[e][f] = 4 * p / 15 + (e == f ? 1 - 16 * p / 15 : 0);
+            D[e][f] = 4.0 / 15 + (e == f ? -16.0 / 15 : 0);
+        }
+    }
+    m->bits[0] = (int)op.targs[0];
+    m->bits[1] = (int)op.targs[1];
+    m->bits[2] = (int)(op.targs[0] + n);
+    m->bits[3] = (int)(op.targs[1] + n);
+    for (int r = 0; r < 16; r++)
+        for (int c = 0; c < 16; c++) {
+            m->st[r][c] = S[c][r];
+            m->d[r][c] = D[r][c];
+        }
+}
+
+// ------------------------------------------------------------- storage
+
+static int ensure_state(State*& s, const Circuit* c, int precision) {
+    if (s && s->precision == precision) return DFS_SUCCESS;
+    if (s) {
+        dfs_state_destroy(static_cast<dfs_state>(s));
+        s = nullptr;
+    }
+    dfs_state out = nullptr;
+    int rc = c->isDM ? dfs_densitymatrix_create(c->numQubits, precision, &out)
+                     : dfs_statevector_create(c->numQubits, precision, &out);
+    if (rc) return rc;
+    s = out;
+    return DFS_SUCCESS;
+}
+
+static int ensure_storage(Circuit* c, int precision) {
+    int rc = ensure_state(c->work, c, precision);
+    if (!rc) rc = ensure_state(c->adj, c, precision);
+    if (rc) return rc;
+    size_t need = 0;
+    for (const CircOp& op : c->ops) need += !op.invertible;
+    for (size_t i = 0; i < c->ckpt.size(); i++)
+        if ((rc = ensure_state(c->ckpt[i], c, precision))) return rc;
+    while (c->ckpt.size() < need) {
+        State* s = nullptr;
+        if ((rc = ensure_state(s, c, precision))) return rc;
+        c->ckpt.push_back(s);
+    }
+    return DFS_SUCCESS;
+}
+
+static unsigned grad_rows(const Circuit* c) {
+    unsigned r = 0;
+    for (const CircOp& op : c->ops) {
+        if (op.param < 0) continue;
+        if (op.kind == OP_PAULI_GADGET || op.kind == OP_PHASE_GADGET) r += c->isDM ? 2 : 1;
+        else if (op.is_channel()) r += 1;
+    }
+    return r;
+}
+
+struct DevLayout {
+    AdjTerm* terms;
+    double2* parts;  // rows x cols
+    double2* sums;   // rows
+    unsigned rows, cols;
+};
+
+static int ensure_dev(Circuit* c, unsigned numTerms, DevLayout* L) {
+    L->rows = grad_rows(c) + 1;  // + the loss row
+    L->cols = adj_partial_cols();
+    size_t tb = ((size_t)numTerms * sizeof(AdjTerm) + 255) & ~(size_t)255;
+    size_t pb = (size_t)L->rows * L->cols * sizeof(double2);
+    size_t need = tb + pb + (size_t)L->rows * sizeof(double2);
+    if (need > c->devBytes) {
+        if (c->dev) {
+            cudaStreamSynchronize(ctx().stream);
+            cudaFree(c->dev);
+            c->dev = nullptr;
+            c->devBytes = 0;
+        }
+        cudaError_t e = cudaMalloc(&c->dev, need);
+        if (e != cudaSuccess) {
+            c->dev = nullptr;
+            return cuda_fail(e, "circuit workspace");
+        }
+        c->devBytes = need;
+    }
+    L->terms = (AdjTerm*)c->dev;
+    L->parts = (double2*)((char*)c->dev + tb);
+    L->sums = L->parts + (size_t)L->rows * L->cols;
+    return DFS_SUCCESS;
+}
+
+static std::vector<AdjTerm> make_terms(unsigned n, const double* coeffs, unsigned T, const unsigned* paulis) {
+    std::vector<AdjTerm> out(T);
+    for (unsigned t = 0; t < T; t++) {
+        AdjTerm a{};
+        int numY = 0;
+        for (unsigned q = 0; q < n; q++) {
+            unsigned p = paulis[(size_t)t * n + q];
+            if (p == 1 || p == 2) a.x |= 1ull << q;
+            if (p == 2 || p == 3) a.yz |= 1ull << q;
+            numY += p == 2;
+        }
+        a.c = coeffs[t];
+        df::f2 s = df::split_const(coeffs[t]);
+        a.cHi = s.hi;
+        a.cLo = s.lo;
+        a.powY = numY & 3;
+        out[t] = a;
+    }
+    return out;
+}
+
+// ---------------------------------------------------------------- passes
+
+static int forward(Circuit* c, State* s, const double* params, bool keepCheckpoints) {
+    size_t k = 0;
+    for (const CircOp& op : c->ops) {
+        int rc;
+        if (!op.invertible && keepCheckpoints) {
+            if ((rc = dfs_state_copy(static_cast<dfs_state>(c->ckpt[k++]), static_cast<dfs_state>(s)))) return rc;
+        }
+        if ((rc = apply_op(s, op, op.val(params), false))) return rc;
+    }
+    return DFS_SUCCESS;
+}
+
+static double im_rot(double2 s, int k) {  // Im(i^k s)
+    switch (k & 3) {
+        case 0: return s.y;
+        case 1: return s.x;
+        case 2: return -s.y;
+        default: return -s.x;
+    }
+}
+
+struct RowUse {
+    int param;
+    int kind;      // 0: gadget (weight * -Im(i^numY S)), 1: channel (Re S)
+    int numY;
+    double weight;
+};
+
+static int backward(Circuit* c, const double* params, double* grad) {
+    DevLayout L;
+    int rc = ensure_dev(c, (unsigned)c->terms.size(), &L);
+    if (rc) return rc;
+    cudaError_t e = cudaMemsetAsync(L.parts, 0, (size_t)L.rows * L.cols * sizeof(double2), ctx().stream);
+    if (e != cudaSuccess) return cuda_fail(e, "gradient table");
+    State* st = c->work;
+    State* ad = c->adj;
+    const unsigned n = c->numQubits;
+    if (c->isDM) {
+        e = cudaMemcpyAsync(L.terms, c->terms.data(), c->terms.size() * sizeof(AdjTerm), cudaMemcpyHostToDevice,
+                            ctx().stream);
+        if (e != cudaSuccess) return cuda_fail(e, "Hamiltonian upload");
+        if ((rc = adj_dm_pauli_sum_build(ad, L.terms, (unsigned)c->terms.size()))) return rc;
+    }
+    std::vector<RowUse> uses;
+    size_t k = c->ckpt.size();
+    for (size_t i = c->ops.size(); i-- > 0;) {
+        const CircOp& op = c->ops[i];
+        const double v = op.val(params);
+        const bool gadget = op.kind == OP_PAULI_GADGET || op.kind == OP_PHASE_GADGET;
+        if (gadget && op.param >= 0) {
+            std::vector<unsigned> ps = op.kind == OP_PAULI_GADGET ? op.paulis : std::vector<unsigned>(op.targs.size(), 3);
+            uint64_t mX, mYZ;
+            int numY;
+            if (c->isDM) {
+                // bra half first: angle -theta (+theta for an odd number of Y)
+                double a = op.kind == OP_PAULI_GADGET && odd_y(ps) ? 1.0 : -1.0;
+                pauli_masks(op.targs, ps, n, &mX, &mYZ, &numY);
+                double2* row = L.parts + (size_t)uses.size() * L.cols;
+                if ((rc = adj_gadget_step(st, ad, mX, mYZ, numY, a * v, row))) return rc;
+                uses.push_back({op.param, 0, numY, a});
+            }
+            pauli_masks(op.targs, ps, 0, &mX, &mYZ, &numY);
+            double2* row = L.parts + (size_t)uses.size() * L.cols;
+            if ((rc = adj_gadget_step(st, ad, mX, mYZ, numY, v, row))) return rc;
+            uses.push_back({op.param, 0, numY, c->isDM ? 1.0 : 2.0});
+            continue;
+        }
+        if (op.is_channel()) {
+            State* before = c->ckpt[--k];
+            if ((rc = dfs_state_copy(static_cast<dfs_state>(st), static_cast<dfs_state>(before)))) return rc;
+            double2* row = nullptr;
+            if (op.param >= 0) {
+                row = L.parts + (size_t)uses.size() * L.cols;
+                uses.push_back({op.param, 1, 0, 1.0});
+            }
+            if (op.kind == OP_DEPH2 || op.kind == OP_DEPOL2) {
+                ChannelMats<2> m;
+                channel_mats2(op, n, v, &m);
+                rc = adj_channel_step(ad, st, nullptr, &m, row);
+            } else {
+                ChannelMats<1> m;
+                channel_mats1(op, n, v, &m);
+                rc = adj_channel_step(ad, st, &m, nullptr, row);
+            }
+            if (rc) return rc;
+            continue;
+        }
+        // unitary (or recorded non-unitary) operations without parameters
+        if ((rc = apply_op(ad, op, v, true))) return rc;
+        if (op.invertible) {
+            if ((rc = apply_op(st, op, v, true))) return rc;
+        } else {
+            State* before = c->ckpt[--k];
+            if ((rc = dfs_state_copy(static_cast<dfs_state>(st), static_cast<dfs_state>(before)))) return rc;
+        }
+    }
+    std::vector<double2> sums(uses.size());
+    if (!uses.empty()) {
+        if ((rc = adj_sum_rows(L.parts, (unsigned)uses.size(), L.cols, L.sums))) return rc;
+        e = cudaMemcpyAsync(sums.data(), L.sums, uses.size() * sizeof(double2), cudaMemcpyDeviceToHost, ctx().stream);
+        if (e != cudaSuccess) return cuda_fail(e, "gradient readback");
+    }
+    e = cudaStreamSynchronize(ctx().stream);
+    if (e != cudaSuccess) return cuda_fail(e, "gradient sweep");
+    for (int p = 0; p < c->numParams; p++) grad[p] = 0.0;
+    for (size_t r = 0; r < uses.size(); r++) {
+        const RowUse& u = uses[r];
+        grad[u.param] += u.kind == 0 ? -u.weight * im_rot(sums[r], u.numY) : sums[r].x;
+    }
+    return DFS_SUCCESS;
+}
+
+static int check_circuit(const Circuit* c) {
+    return c ? DFS_SUCCESS : fail(DFS_ERR_INVALID_ARG, "null circuit");
+}
+
+static int check_state_for(const Circuit* c, const State* s) {
+    if (!s) return fail(DFS_ERR_INVALID_ARG, "null state");
+    if (s->isDM != c->isDM || s->numQubits != c->numQubits)
+        return fail(DFS_ERR_STATE_KIND, "state (%s, %u qubits) does not match the circuit (%s, %u qubits)",
+                    s->isDM ? "density matrix" : "statevector", s->numQubits,
+                    c->isDM ? "density matrix" : "statevector", c->numQubits);
+    return DFS_SUCCESS;
+}
+
+static int check_params(const Circuit* c, const double* params) {
+    if (c->numParams > 0 && !params) return fail(DFS_ERR_INVALID_ARG, "null parameter vector");
+    for (const CircOp& op : c->ops) {
+        if (op.param < 0 || !op.is_channel()) continue;
+        double p = params[op.param];
+        if (!(p >= 0.0 && p <= 1.0)) return fail(DFS_ERR_INVALID_ARG, "probability parameter %d = %g", op.param, p);
+        if (op.kind == OP_DAMPING && !(p < 1.0))
+            return fail(DFS_ERR_INVALID_ARG, "damping probability parameter %d must be below 1", op.param);
+    }
+    return DFS_SUCCESS;
+}
+
+static int add_op(Circuit* c, CircOp&& op) {
+    note_param(c, op.param);
+    c->haveForward = false;
+    c->ops.push_back(std::move(op));
+    return DFS_SUCCESS;
+}
+
+static int add_channel(Circuit* c, OpKind kind, std::vector<unsigned> qs, int param, double prob) {
+    int rc = check_circuit(c);
+    if (rc) return rc;
+    if (!c->isDM) return fail(DFS_ERR_STATE_KIND, "channels need a density-matrix circuit");
+    if ((rc = check_qs(c, qs.data(), (unsigned)qs.size(), false))) return rc;
+    if ((rc = check_param(param, prob, true))) return rc;
+    CircOp op;
+    op.kind = kind;
+    op.targs = std::move(qs);
+    op.param = param;
+    op.value = prob;
+    op.invertible = false;
+    return add_op(c, std::move(op));
+}
+
+}  // namespace dfs
+
+using namespace dfs;
+
+extern "C" {
+
+int dfs_circuit_create(unsigned n, int isDM, dfs_circuit* out) {
+    if (!out) return fail(DFS_ERR_INVALID_ARG, "null output");
+    if (n == 0 || n > (unsigned)(isDM ? kMaxQubits / 2 : kMaxQubits))
+        return fail(DFS_ERR_TOO_LARGE, "unsupported qubit count %u", n);
+    dfs_circuit c = new (std::nothrow) dfs_circuit_s();
+    if (!c) return fail(DFS_ERR_OUT_OF_MEMORY, "host allocation");
+    c->numQubits = n;
+    c->isDM = isDM ? 1 : 0;
+    *out = c;
+    return DFS_SUCCESS;
+}
+
+int dfs_circuit_destroy(dfs_circuit c) {
+    if (!c) return DFS_SUCCESS;
+    if (c->work) dfs_state_destroy(static_cast<dfs_state>(c->work));
+    if (c->adj) dfs_state_destroy(static_cast<dfs_state>(c->adj));
+    for (State* s : c->ckpt) dfs_state_destroy(static_cast<dfs_state>(s));
+    if (c->dev) {
+        cudaStreamSynchronize(ctx().stream);
+        cudaFree(c->dev);
+    }
+    delete c;
+    return DFS_SUCCESS;
+}
+
+int dfs_circuit_num_params(dfs_circuit c, unsigned* out) {
+    int rc = check_circuit(c);
+    if (rc) return rc;
+    if (!out) return fail(DFS_ERR_INVALID_ARG, "null output");
+    *out = (unsigned)c->numParams;
+    return DFS_SUCCESS;
+}
+
+int dfs_circuit_num_ops(dfs_circuit c, unsigned* out) {
+    int rc = check_circuit(c);
+    if (rc) return rc;
+    if (!out) return fail(DFS_ERR_INVALID_ARG, "null output");
+    *out = (unsigned)c->ops.size();
+    return DFS_SUCCESS;
+}
+
+int dfs_circuit_oneTargGate(dfs_circuit c, unsigned target, const double* gate) {
+    int rc = check_circuit(c);
+    if (!rc) rc = check_q(c, target);
+    if (!rc && !gate) rc = fail(DFS_ERR_INVALID_ARG, "null gate");
+    if (rc) return rc;
+    CircOp op;
+    op.kind = OP_ONE_TARG;
+    op.targs = {target};
+    set_gate(op, gate, 2);
+    return add_op(c, std::move(op));
+}
+
+int dfs_circuit_manyCtrlOneTargGate(dfs_circuit c, const unsigned* ctrls, unsigned nc, unsigned target,
+                                    const double* gate) {
+    int rc = check_circuit(c);
+    if (rc) return rc;
+    std::vector<unsigned> all(ctrls, ctrls + (ctrls ? nc : 0));
+    all.push_back(target);
+    if ((rc = check_qs(c, all.data(), (unsigned)all.size(), false))) return rc;
+    if (!gate) return fail(DFS_ERR_INVALID_ARG, "null gate");
+    CircOp op;
+    op.kind = OP_CTRL;
+    op.targs = {target};
+    op.ctrls.assign(ctrls, ctrls + (ctrls ? nc : 0));
+    set_gate(op, gate, 2);
+    return add_op(c, std::move(op));
+}
+
+int dfs_circuit_swapGate(dfs_circuit c, unsigned q1, unsigned q2) {
+    int rc = check_circuit(c);
+    if (!rc) rc = check_q(c, q1);
+    if (!rc) rc = check_q(c, q2);
+    if (rc) return rc;
+    if (q1 == q2) return DFS_SUCCESS;
+    CircOp op;
+    op.kind = OP_SWAP;
+    op.targs = {q1, q2};
+    return add_op(c, std::move(op));
+}
+
+int dfs_circuit_manyTargGate(dfs_circuit c, const unsigned* targs, unsigned k, const double* gate) {
+    int rc = check_circuit(c);
+    if (!rc) rc = check_qs(c, targs, k, false);
+    if (!rc && !gate) rc = fail(DFS_ERR_INVALID_ARG, "null gate");
+    if (!rc && k > 13) rc = fail(DFS_ERR_TOO_LARGE, "manyTargGate supports at most 13 targets (got %u)", k);
+    if (rc) return rc;
+    CircOp op;
+    op.kind = OP_MANY_TARG;
+    op.targs.assign(targs, targs + k);
+    set_gate(op, gate, (size_t)1 << k);
+    return add_op(c, std::move(op));
+}
+
+static int pauli_op(dfs_circuit c, OpKind kind, const unsigned* targs, const unsigned* paulis, unsigned k, int param,
+                    double theta) {
+    int rc = check_circuit(c);
+    if (!rc) rc = check_qs(c, targs, k, true);
+    if (!rc && kind != OP_PHASE_GADGET) {
+        if (k && !paulis) rc = fail(DFS_ERR_INVALID_ARG, "null Pauli codes");
+        for (unsigned i = 0; !rc && i < k; i++)
+            if (paulis[i] > 3) rc = fail(DFS_ERR_INVALID_ARG, "Pauli code %u (expected 0-3)", paulis[i]);
+    }
+    if (!rc) rc = check_param(param, theta, false);
+    if (rc) return rc;
+    CircOp op;
+    op.kind = kind;
+    // identity factors change nothing: drop them
+    for (unsigned i = 0; i < k; i++) {
+        if (kind != OP_PHASE_GADGET && paulis[i] == 0) continue;
+        op.targs.push_back(targs[i]);
+        if (kind != OP_PHASE_GADGET) op.paulis.push_back(paulis[i]);
+    }
+    op.param = param;
+    op.value = theta;
+    return add_op(c, std::move(op));
+}
+
+int dfs_circuit_pauliTensor(dfs_circuit c, const unsigned* targs, const unsigned* paulis, unsigned k) {
+    return pauli_op(c, OP_PAULI_TENSOR, targs, paulis, k, -1, 0.0);
+}
+
+int dfs_circuit_pauliGadget(dfs_circuit c, const unsigned* targs, const unsigned* paulis, unsigned k, int param,
+                            double theta) {
+    return pauli_op(c, OP_PAULI_GADGET, targs, paulis, k, param, theta);
+}
+
+int dfs_circuit_phaseGadget(dfs_circuit c, const unsigned* targs, unsigned k, int param, double theta) {
+    return pauli_op(c, OP_PHASE_GADGET, targs, nullptr, k, param, theta);
+}
+
+int dfs_circuit_oneQubitDephasing(dfs_circuit c, unsigned qb, int param, double prob) {
+    return add_channel(c, OP_DEPH1, {qb}, param, prob);
+}
+int dfs_circuit_twoQubitDephasing(dfs_circuit c, unsigned qb1, unsigned qb2, int param, double prob) {
+    return add_channel(c, OP_DEPH2, {qb1, qb2}, param, prob);
+}
+int dfs_circuit_oneQubitDepolarising(dfs_circuit c, unsigned qb, int param, double prob) {
+    return add_channel(c, OP_DEPOL1, {qb}, param, prob);
+}
+int dfs_circuit_twoQubitDepolarising(dfs_circuit c, unsigned qb1, unsigned qb2, int param, double prob) {
+    return add_channel(c, OP_DEPOL2, {qb1, qb2}, param, prob);
+}
+int dfs_circuit_damping(dfs_circuit c, unsigned qb, int param, double prob) {
+    return add_channel(c, OP_DAMPING, {qb}, param, prob);
+}
+
+int dfs_circuit_apply(dfs_circuit c, dfs_state s, const double* params) {
+    int rc = check_circuit(c);
+    if (!rc) rc = check_state_for(c, s);
+    if (!rc) rc = check_params(c, params);
+    if (rc) return rc;
+    return forward(c, s, params, false);
+}
+
+int dfs_circuit_expec(dfs_circuit c, dfs_state initial, const double* params, const double* coeffs,
+                      unsigned numTerms, const unsigned* allPaulis, double* loss) {
+    int rc = check_circuit(c);
+    if (!rc) rc = check_state_for(c, initial);
+    if (!rc) rc = check_params(c, params);
+    if (!rc && (numTerms == 0 || !coeffs || !allPaulis || !loss))
+        rc = fail(DFS_ERR_INVALID_ARG, "empty Hamiltonian or null output");
+    for (size_t i = 0; !rc && i < (size_t)numTerms * c->numQubits; i++)
+        if (allPaulis[i] > 3) rc = fail(DFS_ERR_INVALID_ARG, "Pauli code %u (expected 0-3)", allPaulis[i]);
+    if (rc) return rc;
+    c->haveForward = false;
+    if ((rc = ensure_storage(c, initial->precision))) return rc;
+    if ((rc = dfs_state_copy(static_cast<dfs_state>(c->work), initial))) return rc;
+    if ((rc = forward(c, c->work, params, true))) return rc;
+    c->terms = make_terms(c->numQubits, coeffs, numTerms, allPaulis);
+    if (c->isDM) {
+        double re = 0, im = 0;
+        if ((rc = dfs_densitymatrix_expecPauliString(static_cast<dfs_state>(c->work), coeffs, numTerms, allPaulis, &re,
+                                                     &im)))
+            return rc;
+        *loss = re;
+    } else {
+        DevLayout L;
+        if ((rc = ensure_dev(c, numTerms, &L))) return rc;
+        cudaError_t e = cudaMemcpyAsync(L.terms, c->terms.data(), numTerms * sizeof(AdjTerm), cudaMemcpyHostToDevice,
+                                        ctx().stream);
+        if (e != cudaSuccess) return cuda_fail(e, "Hamiltonian upload");
+        double2* row = L.parts + (size_t)(L.rows - 1) * L.cols;
+        e = cudaMemsetAsync(row, 0, L.cols * sizeof(double2), ctx().stream);
+        if (e != cudaSuccess) return cuda_fail(e, "loss row");
+        // the adjoint starts as H psi; its inner product with psi is the loss
+        if ((rc = adj_pauli_sum_apply(c->work, c->adj, L.terms, numTerms, row))) return rc;
+        if ((rc = adj_sum_rows(row, 1, L.cols, L.sums + L.rows - 1))) return rc;
+        double2 v;
+        e = cudaMemcpyAsync(&v, L.sums + L.rows - 1, sizeof(double2), cudaMemcpyDeviceToHost, ctx().stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx().stream);
+        if (e != cudaSuccess) return cuda_fail(e, "loss readback");
+        *loss = v.x;
+    }
+    c->fwdParams.assign(params, params + c->numParams);
+    c->haveForward = true;
+    return DFS_SUCCESS;
+}
+
+int dfs_circuit_gradient(dfs_circuit c, const double* params, double* grad) {
+    int rc = check_circuit(c);
+    if (!rc) rc = check_params(c, params);
+    if (!rc && c->numParams > 0 && !grad) rc = fail(DFS_ERR_INVALID_ARG, "null gradient output");
+    if (rc) return rc;
+    if (!c->haveForward || (c->numParams > 0 && memcmp(c->fwdParams.data(), params, c->numParams * sizeof(double)) != 0))
+        return fail(DFS_ERR_INVALID_ARG, "dfs_circuit_gradient needs a dfs_circuit_expec with the same parameters first");
+    c->haveForward = false;  // the sweep rewinds the stored state
+    return backward(c, params, grad);
+}
+
+}  // extern "C"

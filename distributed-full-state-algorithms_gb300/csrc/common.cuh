@@ -68,8 +68,8 @@ struct PolF64 {  // complex128 storage, native FP64 arithmetic
     using R = double;
     struct A { double re, im; };
     static constexpr bool kEmulated = false;
-    static inline K mk(double re, double im) { return {re, im}; }
-    static inline R mkr(double x) { return x; }
+    static HD K mk(double re, double im) { return {re, im}; }
+    static HD R mkr(double x) { return x; }
     static DEV V load(const store* p, size_t i) { double2 v = p[i]; return {v.x, v.y}; }
     static DEV void save(store* p, size_t i, V v) { p[i] = make_double2(v.re, v.im); }
     static DEV A first(K g, V x) { return {fma(g.re, x.re, -g.im * x.im), fma(g.re, x.im, g.im * x.re)}; }
@@ -93,8 +93,8 @@ struct PolDF {  // complex128 storage, double-float arithmetic on the FP32 pipes
     using R = df::f2;
     struct A { df::acc re, im; };
     static constexpr bool kEmulated = true;
-    static inline K mk(double re, double im) { return {df::split_const(re), df::split_const(im)}; }
-    static inline R mkr(double x) { return df::split_const(x); }
+    static HD K mk(double re, double im) { return {df::split_const(re), df::split_const(im)}; }
+    static HD R mkr(double x) { return df::split_const(x); }
     static DEV V load(const store* p, size_t i) {
         uint4 b = reinterpret_cast<const uint4*>(p)[i];
         return {df::decode_words(b.y, b.x), df::decode_words(b.w, b.z)};
@@ -131,8 +131,8 @@ struct PolF32 {  // complex64 storage and FP32 arithmetic
     using R = float;
     struct A { float re, im; };
     static constexpr bool kEmulated = false;
-    static inline K mk(double re, double im) { return {(float)re, (float)im}; }
-    static inline R mkr(double x) { return (float)x; }
+    static HD K mk(double re, double im) { return {(float)re, (float)im}; }
+    static HD R mkr(double x) { return (float)x; }
     static DEV V load(const store* p, size_t i) { float2 v = p[i]; return {v.x, v.y}; }
     static DEV void save(store* p, size_t i, V v) { p[i] = make_float2(v.re, v.im); }
     static DEV A first(K g, V x) { return {fmaf(g.re, x.re, -g.im * x.im), fmaf(g.re, x.im, g.im * x.re)}; }

@@ -213,6 +213,57 @@ int dfs_densitymatrix_trace(dfs_state s, double* out_re, double* out_im);
 int dfs_densitymatrix_expecPauliString_noalloc(dfs_state s, const double* coeffs, unsigned num_terms,
                                                const unsigned* all_paulis, double* out_re, double* out_im);
 
+/* ------------------------------------------- circuits and adjoint gradients
+ * No reference counterpart.  A circuit records a sequence of the operations above
+ * (same arguments, same maths) on a statevector or a density matrix of num_qubits,
+ * with the angle of a pauliGadget / phaseGadget or the probability of a channel
+ * either fixed or read from a parameter vector (param >= 0 selects params[param];
+ * several operations may share a parameter).  The circuit owns its working states,
+ * allocated on first use in the precision of the initial state it is given.
+ *
+ * dfs_circuit_expec runs the circuit on a copy of `initial` and returns
+ * L = <psi|H|psi> (statevector) or L = Re sum_t coeffs[t] Tr(P_t rho) (density matrix),
+ * H = sum_t coeffs[t] P_t with all_paulis as in dfs_densitymatrix_expecPauliString.
+ * It keeps the final state for dfs_circuit_gradient, which returns dL/dparams by the
+ * adjoint method: one backward sweep carrying the state and the adjoint H psi (vec H
+ * for a density matrix).  The state is recomputed by inverse gates; before every
+ * non-invertible operation (a channel, a non-unitary matrix) the forward pass keeps a
+ * checkpoint copy of the state, and the backward sweep restores it.  Gradients of
+ * gadget angles come from the fused kernel that also undoes the gadget; gradients of
+ * channel probabilities from the channel's superoperator derivative.  All sums
+ * accumulate in FP64-class arithmetic whatever the state precision.
+ * dfs_circuit_gradient fails with DFS_ERR_INVALID_ARG unless the latest
+ * dfs_circuit_expec on this circuit used the same params; it consumes that forward. */
+typedef struct dfs_circuit_s* dfs_circuit;
+
+int dfs_circuit_create(unsigned num_qubits, int is_density_matrix, dfs_circuit* out);
+int dfs_circuit_destroy(dfs_circuit c);
+int dfs_circuit_num_params(dfs_circuit c, unsigned* out);
+int dfs_circuit_num_ops(dfs_circuit c, unsigned* out);
+
+int dfs_circuit_oneTargGate(dfs_circuit c, unsigned target, const double* gate2x2);
+int dfs_circuit_manyCtrlOneTargGate(dfs_circuit c, const unsigned* controls, unsigned num_controls, unsigned target,
+                                    const double* gate2x2);
+int dfs_circuit_swapGate(dfs_circuit c, unsigned qb1, unsigned qb2);
+int dfs_circuit_manyTargGate(dfs_circuit c, const unsigned* targets, unsigned num_targets, const double* gate);
+int dfs_circuit_pauliTensor(dfs_circuit c, const unsigned* targets, const unsigned* paulis, unsigned num_targets);
+int dfs_circuit_pauliGadget(dfs_circuit c, const unsigned* targets, const unsigned* paulis, unsigned num_targets,
+                            int param, double theta);
+int dfs_circuit_phaseGadget(dfs_circuit c, const unsigned* targets, unsigned num_targets, int param, double theta);
+/* channels, density-matrix circuits only (twoQubitDepolarising is the trace-preserving channel) */
+int dfs_circuit_oneQubitDephasing(dfs_circuit c, unsigned qb, int param, double prob);
+int dfs_circuit_twoQubitDephasing(dfs_circuit c, unsigned qb1, unsigned qb2, int param, double prob);
+int dfs_circuit_oneQubitDepolarising(dfs_circuit c, unsigned qb, int param, double prob);
+int dfs_circuit_twoQubitDepolarising(dfs_circuit c, unsigned qb1, unsigned qb2, int param, double prob);
+int dfs_circuit_damping(dfs_circuit c, unsigned qb, int param, double prob);
+
+/* applies the circuit to s in place */
+int dfs_circuit_apply(dfs_circuit c, dfs_state s, const double* params);
+int dfs_circuit_expec(dfs_circuit c, dfs_state initial, const double* params, const double* coeffs,
+                      unsigned num_terms, const unsigned* all_paulis, double* loss);
+/* grad receives dfs_circuit_num_params values */
+int dfs_circuit_gradient(dfs_circuit c, const double* params, double* grad);
+
 #ifdef __cplusplus
 }
 #endif
