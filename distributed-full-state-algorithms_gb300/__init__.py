@@ -9,6 +9,6 @@ The directory name is not an importable identifier, so ``__graft_entry__.package
 from .api import *  # noqa: F401,F403
 from .api import __all__ as _api_all
 from ._lib import C128, C128_NATIVE, C64, DfsError, load as load_library
-from .circuit import Circuit, expectation
+from .circuit import Batch, Circuit, expectation
 
-__all__ = list(_api_all) + ["C128", "C128_NATIVE", "C64", "load_library", "Circuit", "expectation"]
+__all__ = list(_api_all) + ["C128", "C128_NATIVE", "C64", "load_library", "Circuit", "Batch", "expectation"]

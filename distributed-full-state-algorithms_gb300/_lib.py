@@ -129,6 +129,19 @@ PROTOTYPES = {
     "dfs_circuit_apply": [_H, _H, _DP],
     "dfs_circuit_expec": [_H, _H, _DP, _DP, _U, _UP, _DP],
     "dfs_circuit_gradient": [_H, _DP, _DP],
+    "dfs_batch_create": [_HP, _U, _I, _HP],
+    "dfs_batch_destroy": [_H],
+    "dfs_batch_num_params": [_H, _UP],
+    "dfs_batch_param_offset": [_H, _U, _UP],
+    "dfs_batch_set_state": [_H, _U, _H],
+    "dfs_batch_set_random": [_H, _U64],
+    "dfs_batch_get_state": [_H, _U, _H],
+    "dfs_batch_set_hamiltonian": [_H, _U, _DP, _U, _UP],
+    "dfs_batch_set_params": [_H, _DP],
+    "dfs_batch_set_shape": [_H, _U, _U],
+    "dfs_batch_get_shape": [_H, _UP, _UP],
+    "dfs_batch_autotune": [_H, _I, _DP],
+    "dfs_batch_run": [_H, _I, _DP, _DP],
     "dfs_error_string": [_I],
     "dfs_last_error": [],
 }

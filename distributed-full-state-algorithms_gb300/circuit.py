@@ -21,7 +21,7 @@ from . import _lib
 from ._lib import DfsError, call
 from .api import DensityMatrix, StateVector, _gate, _uarr
 
-__all__ = ["Circuit", "CircuitExpectation", "expectation"]
+__all__ = ["Circuit", "Batch", "CircuitExpectation", "expectation"]
 
 _DP = C.POINTER(C.c_double)
 
@@ -180,6 +180,88 @@ class Circuit:
     def expectation_and_gradient(self, initial, params, coeffs, allPaulis):
         loss = self.expectation(initial, params, coeffs, allPaulis)
         return loss, self.gradient(params)
+
+
+class Batch:
+    """Many statevector circuits of uneven size, their <H> and adjoint gradients, in
+    one persistent kernel launch replayed from a CUDA graph (``dfs_batch_*``)."""
+
+    def __init__(self, circuits: Sequence[Circuit], precision: str = "c128"):
+        if any(c.densityMatrix for c in circuits):
+            raise DfsError(4, "batched circuits are statevector circuits")
+        arr = (C.c_void_p * len(circuits))(*[c._h.value for c in circuits])
+        h = C.c_void_p()
+        call("dfs_batch_create", arr, len(circuits), _lib.PRECISIONS[precision], C.byref(h))
+        self._h = h
+        self.precision = precision
+        self.numQubits = [c.numQubits for c in circuits]
+        self.numCircuits = len(circuits)
+
+    def free(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.load().dfs_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    @property
+    def numParams(self) -> int:
+        v = C.c_uint()
+        call("dfs_batch_num_params", self._h, C.byref(v))
+        return v.value
+
+    def paramOffset(self, i: int) -> int:
+        v = C.c_uint()
+        call("dfs_batch_param_offset", self._h, int(i), C.byref(v))
+        return v.value
+
+    def setState(self, i: int, state: StateVector) -> None:
+        call("dfs_batch_set_state", self._h, int(i), state.handle)
+
+    def setRandomStates(self, seed: int) -> None:
+        call("dfs_batch_set_random", self._h, int(seed))
+
+    def getState(self, i: int, out: StateVector) -> None:
+        call("dfs_batch_get_state", self._h, int(i), out.handle)
+
+    def setHamiltonian(self, i: int, coeffs, allPaulis) -> None:
+        c = np.ascontiguousarray(np.asarray(coeffs, dtype=np.float64).ravel())
+        codes, num = _uarr(np.asarray(allPaulis).ravel())
+        if num != c.size * self.numQubits[i]:
+            raise DfsError(1, f"{num} Pauli codes for {c.size} terms of {self.numQubits[i]} qubits")
+        call("dfs_batch_set_hamiltonian", self._h, int(i), c.ctypes.data_as(_DP), c.size, codes)
+
+    def setParams(self, params) -> None:
+        p = np.ascontiguousarray(np.asarray(params, dtype=np.float64).ravel())
+        if p.size < self.numParams:
+            raise DfsError(1, f"{p.size} parameters for a batch of {self.numParams}")
+        call("dfs_batch_set_params", self._h, p.ctypes.data_as(_DP))
+
+    def setShape(self, ctasPerSM: int, teamWidth: int) -> None:
+        call("dfs_batch_set_shape", self._h, int(ctasPerSM), int(teamWidth))
+
+    @property
+    def shape(self):
+        a, b = C.c_uint(), C.c_uint()
+        call("dfs_batch_get_shape", self._h, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def autotune(self, gradient: bool = True) -> float:
+        ms = C.c_double()
+        call("dfs_batch_autotune", self._h, 1 if gradient else 0, C.byref(ms))
+        return ms.value
+
+    def run(self, gradient: bool = True):
+        """(losses per circuit, concatenated gradients or None)."""
+        losses = np.zeros(self.numCircuits)
+        grads = np.zeros(max(1, self.numParams))
+        call("dfs_batch_run", self._h, 1 if gradient else 0, losses.ctypes.data_as(_DP),
+             grads.ctypes.data_as(_DP))
+        return losses, (grads[:self.numParams] if gradient else None)
 
 
 def _torch():

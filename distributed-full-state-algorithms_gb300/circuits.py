@@ -143,6 +143,21 @@ def dm_gadget_ansatz(num_qubits: int, layers: int, per_layer: int, seed: int, ma
     return gates
 
 
+def batch_mix(num_circuits: int, min_qubits: int, max_qubits: int, num_gates: int, num_terms: int, seed: int):
+    """Independent circuits for the batched form: qubit counts uniform in
+    [min_qubits, max_qubits], each a ``gate_mix`` of ``num_gates`` gates with its own seed
+    and a ``pauli_sum`` Hamiltonian of ``num_terms`` terms.  Returns a list of
+    (num_qubits, gates, coeffs, paulis)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(num_circuits):
+        n = int(rng.integers(min_qubits, max_qubits + 1))
+        gates = gate_mix(n, num_gates, seed=seed * 1000003 + 2 * i)
+        coeffs, paulis = pauli_sum(n, num_terms, seed=seed * 1000003 + 2 * i + 1)
+        out.append((n, gates, coeffs, paulis))
+    return out
+
+
 PARAM_KINDS = ("pauli_gadget", "phase_gadget", "deph1", "deph2", "depol1", "depol2", "damping")
 
 

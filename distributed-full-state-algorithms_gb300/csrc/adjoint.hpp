@@ -39,6 +39,6 @@ int adj_dm_pauli_sum_build(State* s, const AdjTerm* terms, unsigned numTerms);
 // partial sums of <ad, D rho> into row (when rho and row are given), then ad <- S^T ad
 int adj_channel_step(State* ad, const State* rho, const ChannelMats<1>* m1, const ChannelMats<2>* m2, double2* row);
 // out[r] = sum of row r of parts (rows x cols), in a fixed order
-int adj_sum_rows(const double2* parts, unsigned rows, unsigned cols, double2* out);
+int adj_sum_rows(const double2* parts, unsigned rows, unsigned cols, double2* out, cudaStream_t stream = nullptr);
 
 }  // namespace dfs

@@ -21,58 +21,8 @@
 #include <cstring>
 #include <vector>
 
-#include "adjoint.hpp"
+#include "circuit.hpp"
 
-namespace dfs {
-
-enum OpKind {
-    OP_ONE_TARG,
-    OP_CTRL,
-    OP_SWAP,
-    OP_MANY_TARG,
-    OP_PAULI_TENSOR,
-    OP_PAULI_GADGET,
-    OP_PHASE_GADGET,
-    OP_DEPH1,
-    OP_DEPH2,
-    OP_DEPOL1,
-    OP_DEPOL2,
-    OP_DAMPING,
-};
-
-struct CircOp {
-    OpKind kind;
-    std::vector<unsigned> targs, ctrls, paulis;
-    std::vector<double> gate, gateAdj;  // interleaved row-major, and its conjugate transpose
-    bool invertible = true;             // false: the forward pass keeps a checkpoint
-    int param = -1;
-    double value = 0;
-    double val(const double* params) const { return param >= 0 ? params[param] : value; }
-    bool is_channel() const { return kind >= OP_DEPH1; }
-};
-
-struct Circuit {
-    unsigned numQubits = 0;
-    int isDM = 0;
-    std::vector<CircOp> ops;
-    int numParams = 0;
-    // working storage, allocated on first use
-    State* work = nullptr;
-    State* adj = nullptr;
-    std::vector<State*> ckpt;  // one per non-invertible operation, in order
-    void* dev = nullptr;       // terms | partial rows | row sums
-    size_t devBytes = 0;
-    // the latest forward pass
-    bool haveForward = false;
-    std::vector<double> fwdParams;
-    std::vector<AdjTerm> terms;
-    std::vector<double> coeffs;
-    std::vector<unsigned> paulis;
-};
-
-}  // namespace dfs
-
-struct dfs_circuit_s : dfs::Circuit {};
 
 namespace dfs {
 

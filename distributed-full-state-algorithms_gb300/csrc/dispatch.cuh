@@ -1,6 +1,9 @@
 // dispatch.cuh -- selection of arithmetic policy and index width per state.
 #pragma once
 
+#include <algorithm>
+#include <vector>
+
 #include "engine.hpp"
 
 namespace dfs {

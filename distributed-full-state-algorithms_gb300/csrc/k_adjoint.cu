@@ -362,11 +362,11 @@ int adj_channel_step(State* ad, const State* rho, const ChannelMats<1>* m1, cons
     return dispatch<RunChannelAdj>(ad, ad, rho, m1, m2, row);
 }
 
-int adj_sum_rows(const double2* parts, unsigned rows, unsigned cols, double2* out) {
+int adj_sum_rows(const double2* parts, unsigned rows, unsigned cols, double2* out, cudaStream_t stream) {
     if (rows == 0) return DFS_SUCCESS;
     unsigned threads = 256, warpsPerCta = threads / 32;
     unsigned grid = (rows + warpsPerCta - 1) / warpsPerCta;
-    k_sum_rows<<<grid, threads, 0, ctx().stream>>>(parts, rows, cols, out);
+    k_sum_rows<<<grid, threads, 0, stream ? stream : ctx().stream>>>(parts, rows, cols, out);
     return check_launch("gradient rows");
 }
 

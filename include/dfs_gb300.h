@@ -264,6 +264,40 @@ int dfs_circuit_expec(dfs_circuit c, dfs_state initial, const double* params, co
 /* grad receives dfs_circuit_num_params values */
 int dfs_circuit_gradient(dfs_circuit c, const double* params, double* grad);
 
+/* ------------------------------------------------------ batched circuits
+ * No reference counterpart.  Many independent statevector circuits of uneven qubit
+ * counts (at most 30), each with its own initial state, parameters and Hamiltonian
+ * (at most 64 terms), run as ONE persistent cooperative kernel launch captured in a
+ * CUDA graph: forward pass, <H> and, with with_gradient, the adjoint gradient of
+ * every circuit.  The graph's launch shape -- CTAs per SM and the team width, the
+ * CTAs that stream one circuit together between team barriers -- is set by
+ * dfs_batch_set_shape or measured by dfs_batch_autotune.  Circuits may hold the
+ * unitary operations of the statevector API (dense gates on at most 3 targets,
+ * at most 6 controls); parameters are concatenated circuit by circuit
+ * (dfs_batch_param_offset).  After a run without the gradient, dfs_batch_get_state
+ * returns a circuit's final state (the gradient sweep rewinds it to the initial one).
+ * Results equal per-circuit dfs_circuit_expec / dfs_circuit_gradient within rounding. */
+typedef struct dfs_batch_s* dfs_batch;
+
+int dfs_batch_create(const dfs_circuit* circuits, unsigned num_circuits, int precision, dfs_batch* out);
+int dfs_batch_destroy(dfs_batch b);
+int dfs_batch_num_params(dfs_batch b, unsigned* total);
+int dfs_batch_param_offset(dfs_batch b, unsigned circuit, unsigned* offset);
+/* initial states: copied from a state of the circuit's size and the batch's precision,
+ * or all drawn at once (seeded N(0,1) amplitudes, normalised; circuit i uses seed + i) */
+int dfs_batch_set_state(dfs_batch b, unsigned circuit, dfs_state s);
+int dfs_batch_set_random(dfs_batch b, uint64_t seed);
+int dfs_batch_get_state(dfs_batch b, unsigned circuit, dfs_state out);
+int dfs_batch_set_hamiltonian(dfs_batch b, unsigned circuit, const double* coeffs, unsigned num_terms,
+                              const unsigned* all_paulis);
+int dfs_batch_set_params(dfs_batch b, const double* params);
+int dfs_batch_set_shape(dfs_batch b, unsigned ctas_per_sm, unsigned team_width);
+int dfs_batch_get_shape(dfs_batch b, unsigned* ctas_per_sm, unsigned* team_width);
+/* measures every candidate shape on this batch and keeps the fastest; best_ms may be null */
+int dfs_batch_autotune(dfs_batch b, int with_gradient, double* best_ms);
+/* losses: one per circuit; grads: dfs_batch_num_params values (with_gradient only) */
+int dfs_batch_run(dfs_batch b, int with_gradient, double* losses, double* grads);
+
 #ifdef __cplusplus
 }
 #endif
