@@ -39,6 +39,12 @@ NUM_GATES = 200
 CIRCUIT_SEED = 20240611
 STATE_SEED = 77
 REF_SAMPLE_GATES = 6
+# differentiation form: 24-qubit ansatz of 20 layers x 24 Pauli gadgets, H of 100 terms
+ADJ_QUBITS, ADJ_LAYERS, ADJ_PER_LAYER, ADJ_TERMS = 24, 20, 24, 100
+# batched form: 512 circuits of 10..22 qubits, 50 gates each, H of 32 terms
+BATCH_CIRCUITS, BATCH_MIN_Q, BATCH_MAX_Q, BATCH_GATES, BATCH_TERMS, BATCH_SEED = 512, 10, 22, 50, 32, 2024
+# precision form: 32 qubits, the gate mix plus dense k = 2, 4, 5, 6 gates, H of 100 terms
+PREC_QUBITS, PREC_TERMS, PREC_DENSE = 32, 100, (2, 4, 5, 6)
 
 
 def parse():
@@ -51,6 +57,8 @@ def parse():
     ap.add_argument("--gates", type=int, default=NUM_GATES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the e2e, FP32 and native-FP64 legs")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the adjoint, batched and 32-qubit precision legs")
     return ap.parse_args()
 
 
@@ -408,7 +416,144 @@ def gpu_arm(args, world, rank, local):
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args, circuits, gates)
+    if not args.no_forms:
+        for name, leg in (("adjoint", adjoint_leg), ("batched", batch_leg), ("precision32", precision_leg)):
+            try:
+                result[name] = leg(dfs, circuits)
+            except Exception as e:  # a failing extra leg must not lose the headline line
+                result[name] = {"error": f"{type(e).__name__}: {e}"}
     return result, rank
+
+
+# ------------------------------------------------- forms beyond plain FP64
+
+def _sync_time(dfs, fn):
+    dfs.comm_synch()
+    t0 = time.perf_counter()
+    out = fn()
+    dfs.comm_synch()
+    return (time.perf_counter() - t0) * 1e3, out
+
+
+def adjoint_leg(dfs, circuits):
+    """Full adjoint gradient against one forward pass (same <H>), complex128 and complex64."""
+    n = ADJ_QUBITS
+    gates = circuits.gadget_ansatz(n, ADJ_LAYERS, ADJ_PER_LAYER, seed=CIRCUIT_SEED)
+    coeffs, paulis = circuits.pauli_sum(n, ADJ_TERMS, seed=7)
+    circ, params = circuits.record(dfs, n, gates)
+    out = {"workload": f"sv{n} ansatz {ADJ_LAYERS}x{ADJ_PER_LAYER} Pauli gadgets ({params.size} parameters), "
+                       f"H of {ADJ_TERMS} terms; forward = circuit + H psi + <H>; gradient = forward + backward"}
+    grads = {}
+    for prec in ("c128", "c64"):
+        init = dfs.StateVector(n, precision=prec)
+        init.setRandomAmps(seed=STATE_SEED, normalise=True)
+        circ.expectation(init, params, coeffs, paulis)
+        circ.gradient(params)
+        fw, bw, plain = [], [], []
+        work = dfs.StateVector(n, precision=prec)
+        for _ in range(3):
+            fw.append(_sync_time(dfs, lambda: circ.expectation(init, params, coeffs, paulis))[0])
+            ms, grads[prec] = _sync_time(dfs, lambda: circ.gradient(params))
+            bw.append(ms)
+            work.copyFrom(init)
+            plain.append(_sync_time(dfs, lambda: (circ.apply(work, params),
+                                                  dfs.statevector_expecPauliSum(work, coeffs, paulis)))[0])
+        f, b, p = statistics.median(fw), statistics.median(bw), statistics.median(plain)
+        out[prec] = {"forward_ms": f, "backward_ms": b, "gradient_over_forward": (f + b) / f,
+                     "gradient_over_plain_forward": (f + b) / p, "plain_forward_ms": p}
+        init.free()
+        work.free()
+    scale = float(np.max(np.abs(grads["c128"])))
+    out["c64_gradient_max_rel_err"] = float(np.max(np.abs(grads["c64"] - grads["c128"]))) / scale
+    return out
+
+
+def batch_bytes(specs, circuits, elem):
+    """Algorithmic bytes of one batched run with gradients: the initial-state copy, each
+    gate, H psi (T reads, the loss read, one write), and each gate's backward step (the
+    state and the adjoint)."""
+    total = 0
+    for n, gates, coeffs, _ in specs:
+        N = 1 << n
+        total += 2 * N * elem + (len(coeffs) + 2) * N * elem
+        for g in gates:
+            fb = circuits.algorithmic_bytes(g, N, elem)
+            total += fb + 2 * fb
+    return total
+
+
+def batch_leg(dfs, circuits):
+    """One persistent launch (graph replay) for every circuit's <H> and gradient, against
+    per-circuit runs through the circuit runtime."""
+    specs = circuits.batch_mix(BATCH_CIRCUITS, BATCH_MIN_Q, BATCH_MAX_Q, BATCH_GATES, BATCH_TERMS, BATCH_SEED)
+    recs = [circuits.record(dfs, n, g, parametrise=("pauli_gadget", "phase_gadget")) for n, g, _, _ in specs]
+    circs = [r[0] for r in recs]
+    params = [r[1] for r in recs]
+    out = {"workload": f"{BATCH_CIRCUITS} statevector circuits of {BATCH_MIN_Q}-{BATCH_MAX_Q} qubits, "
+                       f"{BATCH_GATES} gates each, H of {BATCH_TERMS} terms, <H> and adjoint gradient per circuit",
+           "total_amplitudes": int(sum(1 << s[0] for s in specs))}
+    for prec, elem in (("c128", 16), ("c64", 8)):
+        b = dfs.Batch(circs, precision=prec)
+        for i, (n, _, c, p) in enumerate(specs):
+            b.setHamiltonian(i, c, p)
+        b.setRandomStates(seed=STATE_SEED)
+        b.setParams(np.concatenate(params))
+        t0 = time.perf_counter()
+        b.autotune(gradient=True)
+        tune_s = time.perf_counter() - t0
+        b.run(gradient=True)
+        runs = [_sync_time(dfs, lambda: b.run(gradient=True))[0] for _ in range(3)]
+        batch_ms = statistics.median(runs)
+        cps, width = b.shape
+        b.free()
+        inits = []
+        for i, (n, _, c, p) in enumerate(specs):
+            s0 = dfs.StateVector(n, precision=prec)
+            s0.setRandomAmps(seed=STATE_SEED + i, normalise=True)
+            inits.append(s0)
+
+        def sequential():
+            for i, (n, _, c, p) in enumerate(specs):
+                circs[i].expectation(inits[i], params[i], c, p)
+                circs[i].gradient(params[i])
+
+        sequential()
+        seq_ms = min(_sync_time(dfs, sequential)[0] for _ in range(2))
+        for s0 in inits:
+            s0.free()
+        nbytes = batch_bytes(specs, circuits, elem)
+        out[prec] = {"batch_ms": batch_ms, "sequential_ms": seq_ms, "speedup": seq_ms / batch_ms,
+                     "shape": {"ctas_per_sm": cps, "team_width": width}, "autotune_s": tune_s,
+                     "algorithmic_gb": nbytes / 1e9, "gbs_algorithmic": nbytes / (batch_ms * 1e-3) / 1e9}
+    return out
+
+
+def precision_leg(dfs, circuits):
+    """complex64 against complex128 at 32 qubits: time, <H> error and fidelity; the
+    complex128 engine (parity-pinned to the oracle) stands for the FP64 reference."""
+    n = PREC_QUBITS
+    gates = circuits.gate_mix(n, NUM_GATES, CIRCUIT_SEED, dense_k=PREC_DENSE)
+    coeffs, paulis = circuits.pauli_sum(n, PREC_TERMS, seed=7)
+    res = {"workload": f"sv{n} gate mix + dense k={list(PREC_DENSE)}, {NUM_GATES} gates, H of {PREC_TERMS} terms"}
+    states, expec = {}, {}
+    for prec in ("c128", "c64"):
+        s0 = dfs.StateVector(n, precision=prec)
+        s0.setRandomAmps(seed=STATE_SEED, normalise=True)
+        ms, _ = _sync_time(dfs, lambda: circuits.apply(dfs, s0, gates))
+        expec[prec] = dfs.statevector_expecPauliSum(s0, coeffs, paulis).real
+        res[prec] = {"gates_per_s": len(gates) / (ms * 1e-3), "ms": ms}
+        states[prec] = s0
+    conv = dfs.StateVector(n, precision="c128")
+    conv.copyFrom(states["c64"])
+    ip = dfs.inner_product(states["c128"], conv)
+    fid = abs(ip) ** 2 / (dfs.norm_squared(states["c128"]) * dfs.norm_squared(conv))
+    for s0 in list(states.values()) + [conv]:
+        s0.free()
+    res["c64_speedup"] = res["c64"]["gates_per_s"] / res["c128"]["gates_per_s"]
+    res["expec_abs_err"] = abs(expec["c64"] - expec["c128"])
+    res["expec_rel_err"] = res["expec_abs_err"] / float(np.sum(np.abs(coeffs)))
+    res["fidelity"] = fid
+    return res
 
 
 def cpu_baseline(args, circuits, gates):

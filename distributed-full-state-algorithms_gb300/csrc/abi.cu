@@ -341,9 +341,8 @@ int dfs_state_copy(dfs_state dst, dfs_state src) {
     if (rc) return rc;
     if (dst->numAmps != src->numAmps || dst->isDM != src->isDM || dst->numQubits != src->numQubits)
         return fail(DFS_ERR_INVALID_ARG, "states differ in shape");
-    if (elem_bytes(dst->precision) != elem_bytes(src->precision))
-        return fail(DFS_ERR_PRECISION, "states differ in precision");
     if (dst == src) return DFS_SUCCESS;
+    if (elem_bytes(dst->precision) != elem_bytes(src->precision)) return state_convert(dst, src);
     cudaError_t e = cudaMemcpyAsync(dst->amps, src->amps, src->numAmps * elem_bytes(src->precision),
                                     cudaMemcpyDeviceToDevice, g_ctx.stream);
     return e == cudaSuccess ? DFS_SUCCESS : cuda_fail(e, "state copy");

@@ -84,6 +84,7 @@ int dm_partial_trace(State* in, const unsigned* targs, unsigned k, State* out);
 int state_fill_zero(State* s);
 int state_set_classical(State* s, uint64_t index);
 int state_set_random(State* s, uint64_t seed, int normalise);
+int state_convert(State* dst, const State* src);  // complex64 <-> complex128 storage
 int state_upload(State* s, const double* amps, uint64_t start, uint64_t count);
 int state_download(State* s, double* amps, uint64_t start, uint64_t count);
 int sv_expec_pauli_sum(State* s, const double* coeffs, unsigned numTerms, const unsigned* allPaulis, double* re,

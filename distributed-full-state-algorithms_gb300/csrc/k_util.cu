@@ -115,6 +115,31 @@ int state_set_random(State* s, uint64_t seed, int normalise) {
     return state_scale_real(s, 1.0 / std::sqrt(n2));
 }
 
+// ------------------------------------------------------ precision change
+// complex64 <-> complex128 storage: exact widening, round-to-nearest narrowing
+
+template <class D, class S>
+__global__ void __launch_bounds__(kThreads) k_convert(D* __restrict__ dst, const S* __restrict__ src, uint64_t n) {
+    for (uint64_t j = (uint64_t)blockIdx.x * kThreads + threadIdx.x; j < n; j += (uint64_t)gridDim.x * kThreads) {
+        S v = src[j];
+        D o;
+        o.x = v.x;
+        o.y = v.y;
+        dst[j] = o;
+    }
+}
+
+int state_convert(State* dst, const State* src) {
+    Launch L = launch_for(src->numAmps, 1, ctx().numSMs);
+    if (src->precision == DFS_C64)
+        k_convert<double2, float2><<<L.grid, L.block, 0, ctx().stream>>>((double2*)dst->amps, (const float2*)src->amps,
+                                                                          src->numAmps);
+    else
+        k_convert<float2, double2><<<L.grid, L.block, 0, ctx().stream>>>((float2*)dst->amps, (const double2*)src->amps,
+                                                                          src->numAmps);
+    return check_launch("precision conversion");
+}
+
 // ------------------------------------------------------------- reductions
 // k_reduce<P, IT, Op>: each CTA accumulates op.add(j, sum) over a grid-stride
 // range of items and writes one complex partial; the host adds the partials.

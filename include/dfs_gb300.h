@@ -112,7 +112,9 @@ int dfs_state_get_amps(dfs_state s, double* amps, uint64_t start, uint64_t count
 /* same, from/to host memory in the state's own device format (no conversion) */
 int dfs_state_set_raw(dfs_state s, const void* src, uint64_t start, uint64_t count);
 int dfs_state_get_raw(dfs_state s, void* dst, uint64_t start, uint64_t count);
-/* device-to-device copy between two states of equal shape and precision */
+/* device-to-device copy between two states of equal shape; between complex64 and
+ * complex128 storage the amplitudes are converted (exact widening, round-to-nearest
+ * narrowing) */
 int dfs_state_copy(dfs_state dst, dfs_state src);
 /* zero all amplitudes */
 int dfs_state_set_zero(dfs_state s);
