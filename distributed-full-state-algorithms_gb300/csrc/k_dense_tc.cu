@@ -16,8 +16,9 @@
 //    real of a group is scaled by the group's largest power of two and cut into
 //    six 8-bit integer slices (48 bits), each an exact bf16; every gate row is
 //    cut the same way with its own power of two.  A slice product summed over
-//    K <= 32 terms is an integer below 2^21 and the <= 6 products of equal
-//    weight 2^-8u below 2^24, so the FP32 tensor-core accumulation is exact.
+//    K <= 64 terms is an integer below 2^22, and the accumulators of weights
+//    2^0 .. 2^-24 (1 to 4 products) stay below 2^24, so the FP32 tensor-core
+//    accumulation is exact there.
 //    The 21 products with s + t <= 5 go to five TMEM accumulators (the two
 //    lowest weights share one, with B pre-scaled); the epilogue sums them in
 //    double-float (two exact TwoSums, the rest into the error term) and rounds
@@ -57,11 +58,14 @@ struct Dense {
     static constexpr uint32_t KG16 = R / 8;     // core matrices along K
     static constexpr uint32_t A16 = 128 * R * 2;
     static constexpr uint32_t B16 = R * R * 2;
-    static constexpr uint32_t COLS64 = (kOzAccs * R <= 64) ? 64 : (kOzAccs * R <= 128 ? 128 : 256);
-    static_assert(kOzAccs * R <= 256, "TMEM budget");
-    // tf32 operands (complex64 path)
+    static constexpr uint32_t COLS64 =
+        (kOzAccs * R <= 64) ? 64 : (kOzAccs * R <= 128 ? 128 : (kOzAccs * R <= 256 ? 256 : 512));
+    static constexpr bool kOzakiFits = kOzAccs * R <= 512;  // TMEM columns of one SM
+    // tf32 operands (complex64 path); A is staged KCH32 chunks of K at a time so that
+    // A chunk + the whole B (big and small) fit in shared memory at k = 6
     static constexpr uint32_t KG32 = R / 4;
-    static constexpr uint32_t A32 = 128 * R * 4;
+    static constexpr int KCH32 = KT >= 6 ? 2 : 1;
+    static constexpr uint32_t A32 = 128 * (R / KCH32) * 4;
     static constexpr uint32_t B32 = R * R * 4;
     static constexpr uint32_t COLS32 = R < 32 ? 32 : R;
 };
@@ -98,9 +102,10 @@ DEV float float_of_byte(uint32_t word, uint32_t magicBits, float magic) {
 DEV uint32_t pack_bf16(float lo, float hi) { return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632u); }
 
 template <class IT, int KT>
-__global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : 2) k_dense_ozaki(uint4* __restrict__ amps, IT numGroups,
+__global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1)) k_dense_ozaki(uint4* __restrict__ amps, IT numGroups,
                                                                 DenseParams<IT, KT> p, const uint4* __restrict__ bsl) {
     using S = Dense<KT>;
+    static_assert(S::kOzakiFits, "TMEM budget");
     constexpr int D = S::D, R = S::R, kHalf = D / 2;  // amplitudes per thread
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* sA = smem;
@@ -220,35 +225,39 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : 2) k_dense_ozaki
 
         // ---- y_n = 2^(E + e_n - 1038) * sum_u D_u[n] 2^(-8u), summed in double-float: D_0,
         //      D_1 2^-8 and D_2 2^-16 exactly (TwoSum), the rest into the error term
-        float acc[kOzAccs][D];
+        // in chunks of 8 output reals (4 amplitudes) so that large D stays in registers
         const uint32_t lane = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(half * D);
 #pragma unroll
-        for (int u = 0; u < kOzAccs; u++) {
-            float v[16];
-            if (D >= 16) tc::ld16(lane + (uint32_t)(u * R), v);
-            else tc::ld8(lane + (uint32_t)(u * R), v);
+        for (int ch = 0; ch < D / 8; ch++) {
+            float acc[kOzAccs][8];
+#pragma unroll
+            for (int u = 0; u < kOzAccs; u++) {
+                float v[16];
+                tc::ld8(lane + (uint32_t)(u * R + ch * 8), v);
+#pragma unroll
+                for (int j = 0; j < 8; j++) acc[u][j] = v[j];
+            }
             tc::ld_wait();
+            if (valid) {
 #pragma unroll
-            for (int j = 0; j < D; j++) acc[u][j] = v[j];
-        }
-        if (valid) {
+                for (int c4 = 0; c4 < 4; c4++) {
+                    const int c = ch * 4 + c4;
+                    uint32_t w[4];
 #pragma unroll
-            for (int c = 0; c < kHalf; c++) {
-                uint32_t w[4];
-#pragma unroll
-                for (int part = 0; part < 2; part++) {
-                    const int j = 2 * c + part;
-                    df::f2 t = df::two_sum(acc[0][j], acc[1][j] * 0x1p-8f);
-                    df::f2 t2 = df::two_sum(t.hi, acc[2][j] * 0x1p-16f);
-                    float e = df::add_rn(t.lo, t2.lo);
-                    e = __fmaf_rn(acc[3][j], 0x1p-24f, e);
-                    e = __fmaf_rn(acc[4][j], 0x1p-32f, e);
-                    df::f2 y = df::fast_two_sum(t2.hi, e);
-                    // times 2^(E + e_n - 1038), folded into the exponent field
-                    df::encode_words_scaled(y, (int)E + p.colExp[half * D + j] - 1038, &w[2 * part + 1],
-                                            &w[2 * part]);
+                    for (int part = 0; part < 2; part++) {
+                        const int j = 2 * c4 + part;
+                        df::f2 t = df::two_sum(acc[0][j], acc[1][j] * 0x1p-8f);
+                        df::f2 t2 = df::two_sum(t.hi, acc[2][j] * 0x1p-16f);
+                        float e = df::add_rn(t.lo, t2.lo);
+                        e = __fmaf_rn(acc[3][j], 0x1p-24f, e);
+                        e = __fmaf_rn(acc[4][j], 0x1p-32f, e);
+                        df::f2 y = df::fast_two_sum(t2.hi, e);
+                        // times 2^(E + e_n - 1038), folded into the exponent field
+                        df::encode_words_scaled(y, (int)E + p.colExp[half * D + 2 * c + part] - 1038,
+                                                &w[2 * part + 1], &w[2 * part]);
+                    }
+                    amps[base + p.off[half * kHalf + c]] = make_uint4(w[0], w[1], w[2], w[3]);
                 }
-                amps[base + p.off[half * kHalf + c]] = make_uint4(w[0], w[1], w[2], w[3]);
             }
         }
 #pragma unroll
@@ -272,10 +281,12 @@ __global__ void __launch_bounds__(kTcThreads) k_dense_3xtf32(float2* __restrict_
                                                              DenseParams<IT, KT> p, const uint4* __restrict__ bsl) {
     using S = Dense<KT>;
     constexpr int D = S::D, R = S::R;
+    constexpr int KCH = S::KCH32, RC = R / KCH, DC = D / KCH;  // K chunks, reals / amplitudes per chunk
+    constexpr uint32_t KGA = RC / 4;                            // A core matrices along K
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* sAbig = smem;
     unsigned char* sAsmall = smem + S::A32;
-    unsigned char* sB = smem + 2 * S::A32;  // big then small
+    unsigned char* sB = smem + 2 * S::A32;  // big then small, the whole of K
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmemSlot;
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -289,71 +300,81 @@ __global__ void __launch_bounds__(kTcThreads) k_dense_3xtf32(float2* __restrict_
     const uint32_t tmem = tmemSlot;
     const uint32_t id = tc::idesc(2, R);
     uint32_t phase = 0;
+    bool timedOut = false;
     const IT numTiles = (numGroups + 127) / 128;
 
-    for (IT tile = blockIdx.x; tile < numTiles; tile += gridDim.x) {
+    for (IT tile = blockIdx.x; tile < numTiles && !timedOut; tile += gridDim.x) {
         const IT g = tile * 128 + (IT)tid;
         const bool valid = g < numGroups;
         const IT base = valid ? insert_zeros(g, p.q) : (IT)0;
-        float x[R];  // reals ordered [re x0, im x0, re x1, ...]
+        float2 xv[DC];  // this chunk's amplitudes; reals ordered [re x0, im x0, re x1, ...]
 #pragma unroll
-        for (int c = 0; c < D; c++) {
-            float2 v = valid ? amps[base + p.off[c]] : make_float2(0.f, 0.f);
-            x[2 * c] = v.x;
-            x[2 * c + 1] = v.y;
-        }
+        for (int c = 0; c < DC; c++) xv[c] = valid ? amps[base + p.off[c]] : make_float2(0.f, 0.f);
+#pragma unroll 1
+        for (int ch = 0; ch < KCH; ch++) {
 #pragma unroll
-        for (int kg = 0; kg < R / 4; kg++) {
-            uint32_t big[4], small[4];
+            for (int kg = 0; kg < RC / 4; kg++) {
+                uint32_t big[4], small[4];
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                float v = x[kg * 4 + j];
-                big[j] = to_tf32(v);
-                small[j] = to_tf32(__fsub_rn(v, __uint_as_float(big[j])));
+                for (int j = 0; j < 4; j++) {
+                    const int r = kg * 4 + j;
+                    const float v = (r & 1) ? xv[r >> 1].y : xv[r >> 1].x;
+                    big[j] = to_tf32(v);
+                    small[j] = to_tf32(__fsub_rn(v, __uint_as_float(big[j])));
+                }
+                const uint32_t off = tc::kmajor_offset(tid, kg * 4, KGA, 4);
+                *reinterpret_cast<uint4*>(sAbig + off) = make_uint4(big[0], big[1], big[2], big[3]);
+                *reinterpret_cast<uint4*>(sAsmall + off) = make_uint4(small[0], small[1], small[2], small[3]);
             }
-            const uint32_t off = tc::kmajor_offset(tid, kg * 4, S::KG32, 4);
-            *reinterpret_cast<uint4*>(sAbig + off) = make_uint4(big[0], big[1], big[2], big[3]);
-            *reinterpret_cast<uint4*>(sAsmall + off) = make_uint4(small[0], small[1], small[2], small[3]);
-        }
-        tc::fence_smem_to_async();
-        tc::fence_before_sync();
-        __syncthreads();
-        tc::fence_after_sync();
-        if (tid == 0) {
-            const uint32_t lbo = 128, sbo = 128 * S::KG32;
+            tc::fence_smem_to_async();
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+            if (tid == 0) {
 #pragma unroll
-            for (int ks = 0; ks < R / 8; ks++) {
-                uint64_t ab = tc::desc(tc::smem_u32(sAbig + ks * 256), lbo, sbo);
-                uint64_t as = tc::desc(tc::smem_u32(sAsmall + ks * 256), lbo, sbo);
-                uint64_t bb = tc::desc(tc::smem_u32(sB + ks * 256), lbo, sbo);
-                uint64_t bs = tc::desc(tc::smem_u32(sB + S::B32 + ks * 256), lbo, sbo);
-                tc::mma_tf32(tmem, as, bb, id, ks > 0 ? 1u : 0u);
-                tc::mma_tf32(tmem, ab, bs, id, 1u);
-                tc::mma_tf32(tmem, ab, bb, id, 1u);
+                for (int ks = 0; ks < RC / 8; ks++) {
+                    const int kAll = ch * (RC / 8) + ks;  // K step within the whole of K (B)
+                    uint64_t ab = tc::desc(tc::smem_u32(sAbig + ks * 256), 128, 128 * KGA);
+                    uint64_t as = tc::desc(tc::smem_u32(sAsmall + ks * 256), 128, 128 * KGA);
+                    uint64_t bb = tc::desc(tc::smem_u32(sB + kAll * 256), 128, 128 * S::KG32);
+                    uint64_t bs = tc::desc(tc::smem_u32(sB + S::B32 + kAll * 256), 128, 128 * S::KG32);
+                    tc::mma_tf32(tmem, as, bb, id, kAll > 0 ? 1u : 0u);
+                    tc::mma_tf32(tmem, ab, bs, id, 1u);
+                    tc::mma_tf32(tmem, ab, bb, id, 1u);
+                }
+                tc::commit(&mbar);
             }
-            tc::commit(&mbar);
+            // the next chunk's amplitudes load while the tensor cores work on this one
+            if (ch + 1 < KCH) {
+#pragma unroll
+                for (int c = 0; c < DC; c++)
+                    xv[c] = valid ? amps[base + p.off[(ch + 1) * DC + c]] : make_float2(0.f, 0.f);
+            }
+            const bool ok = tc::mbar_wait(&mbar, phase, kTcWaitLimit);
+            phase ^= 1u;
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) atomicExch(&g_tcTimeout, 1);
+                timedOut = true;
+                break;
+            }
+            tc::fence_after_sync();
         }
-        const bool ok = tc::mbar_wait(&mbar, phase, kTcWaitLimit);
-        phase ^= 1u;
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0) atomicExch(&g_tcTimeout, 1);
-            break;
-        }
-        tc::fence_after_sync();
-        float y[R];
+        if (timedOut) break;
         const uint32_t lane = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll
         for (int nc = 0; nc < R / 16; nc++) {
             float v[16];
             tc::ld16(lane + (uint32_t)(nc * 16), v);
             tc::ld_wait();
+            if (valid) {
 #pragma unroll
-            for (int j = 0; j < 16; j++) y[nc * 16 + j] = v[j];
+                for (int j = 0; j < 8; j++) amps[base + p.off[nc * 8 + j]] = make_float2(v[2 * j], v[2 * j + 1]);
+            }
         }
-        if (valid) {
-#pragma unroll
-            for (int c = 0; c < D; c++) amps[base + p.off[c]] = make_float2(y[2 * c], y[2 * c + 1]);
-        }
+        // every thread's TMEM reads of this tile precede the next tile's MMAs
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -469,11 +490,16 @@ static int dense_tc_run(State* s, const unsigned* targs, const double* g) {
         prepare_tf32_b<KT>(g, bytes);
         smem = 2 * S::A32 + 2 * S::B32;
         ctasPerSM = (int)std::min<uint32_t>(4, 512 / S::COLS32);
-    } else {
+    } else if constexpr (S::kOzakiFits) {
         prepare_ozaki_b<KT>(g, bytes, p.colExp);
         smem = kOzSlices * S::A16 + kOzBCopies * kOzSlices * S::B16;
         ctasPerSM = (int)(512 / S::COLS64);
+    } else {
+        return fail(DFS_ERR_INVALID_ARG, "no complex128 tensor-core path for %d targets", KT);
     }
+    // no more CTAs per SM than shared memory holds (1 KiB reserved per CTA, static <= 2 KiB)
+    ctasPerSM = (int)std::max<size_t>(1, std::min<size_t>((size_t)ctasPerSM,
+                                                          (ctx().smemOptin + 1024) / (smem + 3 * 1024)));
     // at most ctasPerSM CTAs may share an SM's 512 TMEM columns: pad the dynamic shared
     // memory so that ctasPerSM + 1 cannot be resident (each also holds <= 2 KiB static
     // + 1 KiB reserved)
@@ -490,7 +516,7 @@ static int dense_tc_run(State* s, const unsigned* targs, const double* g) {
         auto kern = k_dense_3xtf32<IT, KT>;
         if ((rc = set_smem(kern, smem))) return rc;
         kern<<<grid, kTcThreads, smem, ctx().stream>>>((float2*)s->amps, groups, p, (const uint4*)ctx().scratch);
-    } else {
+    } else if constexpr (S::kOzakiFits) {
         auto kern = k_dense_ozaki<IT, KT>;
         if ((rc = set_smem(kern, smem))) return rc;
         kern<<<grid, 2 * kTcThreads, smem, ctx().stream>>>((uint4*)s->amps, groups, p, (const uint4*)ctx().scratch);
@@ -499,11 +525,13 @@ static int dense_tc_run(State* s, const unsigned* targs, const double* g) {
 }
 
 // measured at 30 qubits: complex128 k=3 3.4 TB/s (CUDA cores 2.4), k=4 3.2 (0.75);
-// complex64 k=4 5.2 TB/s (0.9), while k=3 stays on the FP32 CUDA cores (6.0 vs 4.9)
+// complex64 k=4 5.2 TB/s (0.9), while k=3 stays on the FP32 CUDA cores (6.0 vs 4.9).
+// k = 5 (both) and k = 6 (complex64, A staged in two K halves) follow the same kernels;
+// complex128 k = 6 would need 192 KB of A slices and 393 KB of B slices per tile.
 bool dense_tc_supported(const State* s, unsigned k) {
     if (s->precision == DFS_C128_NATIVE || !ctx().denseTensorCores) return false;
-    if (s->precision == DFS_C64) return k == 4;
-    return k == 3 || k == 4;
+    if (s->precision == DFS_C64) return k >= 4 && k <= 6;
+    return k >= 3 && k <= 5;
 }
 
 int dense_tc(State* s, const unsigned* targs, unsigned k, const double* gate) {
@@ -511,8 +539,13 @@ int dense_tc(State* s, const unsigned* targs, unsigned k, const double* gate) {
     switch (k) {
         case 3: return wide ? dense_tc_run<uint64_t, 3>(s, targs, gate) : dense_tc_run<uint32_t, 3>(s, targs, gate);
         case 4: return wide ? dense_tc_run<uint64_t, 4>(s, targs, gate) : dense_tc_run<uint32_t, 4>(s, targs, gate);
-        default: return fail(DFS_ERR_INVALID_ARG, "no tensor-core path for %u targets", k);
+        case 5: return wide ? dense_tc_run<uint64_t, 5>(s, targs, gate) : dense_tc_run<uint32_t, 5>(s, targs, gate);
+        case 6:
+            if (s->precision != DFS_C64) break;
+            return wide ? dense_tc_run<uint64_t, 6>(s, targs, gate) : dense_tc_run<uint32_t, 6>(s, targs, gate);
+        default: break;
     }
+    return fail(DFS_ERR_INVALID_ARG, "no tensor-core path for %u targets", k);
 }
 
 int dense_tc_status() {

@@ -192,7 +192,7 @@ def test_reductions_sv(dfs, oracle, rng):
 
 
 @pytest.mark.parametrize("prec", PRECISIONS)
-@pytest.mark.parametrize("k", [3, 4])
+@pytest.mark.parametrize("k", [3, 4, 5, 6])
 def test_dense_gate_extreme_magnitudes(dfs, oracle, prec, k, rng):
     """The tensor-core dense path scales each group by its largest power of two:
     groups mixing 1e-30 and 1, exact zeros, negative zeros and whole zero groups
