@@ -158,26 +158,35 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
         for (int kg = 0; kg < D / 8; kg++) {
             uint32_t packed[kOzSlices][4];
 #pragma unroll
-            for (int j = 0; j < 4; j++) {  // amplitude kg*4 + j: reals (re, im)
+            for (int j = 0; j < 4; j++) {  // amplitude kg*4 + j: reals (re, im), sliced as a pair
                 const uint4 v = cur[kg * 4 + j];
-                float f[2][kOzSlices];
+                const uint64_t F0 = fraction48(v.y, v.x, E), F1 = fraction48(v.w, v.z, E);
+                const uint32_t Fh0 = (uint32_t)(F0 >> 32), Fl0 = (uint32_t)F0;
+                const uint32_t Fh1 = (uint32_t)(F1 >> 32), Fl1 = (uint32_t)F1;
+                const uint32_t mb0 = (v.y >> 31) ? 0xCB000000u : 0x4B000000u;
+                const uint32_t mb1 = (v.w >> 31) ? 0xCB000000u : 0x4B000000u;
+                const uint64_t magic = tc::pk2(__uint_as_float(mb0), __uint_as_float(mb1));
+                // sign * byte as an exact float: the byte under the exponent of +-2^23
+                // (one PRMT per real), minus +-2^23 (one f32x2 subtraction per pair)
+                uint32_t m0[kOzSlices], m1[kOzSlices];
+                m0[0] = __byte_perm(Fh0, mb0, 0x7651u);
+                m0[1] = __byte_perm(Fh0, mb0, 0x7650u);
+                m0[2] = __byte_perm(Fl0, mb0, 0x7653u);
+                m0[3] = __byte_perm(Fl0, mb0, 0x7652u);
+                m0[4] = __byte_perm(Fl0, mb0, 0x7651u);
+                m0[5] = __byte_perm(Fl0, mb0, 0x7650u);
+                m1[0] = __byte_perm(Fh1, mb1, 0x7651u);
+                m1[1] = __byte_perm(Fh1, mb1, 0x7650u);
+                m1[2] = __byte_perm(Fl1, mb1, 0x7653u);
+                m1[3] = __byte_perm(Fl1, mb1, 0x7652u);
+                m1[4] = __byte_perm(Fl1, mb1, 0x7651u);
+                m1[5] = __byte_perm(Fl1, mb1, 0x7650u);
 #pragma unroll
-                for (int part = 0; part < 2; part++) {
-                    const uint32_t H = part ? v.w : v.y, L = part ? v.z : v.x;
-                    uint64_t F = fraction48(H, L, E);
-                    uint32_t Fh = (uint32_t)(F >> 32), Fl = (uint32_t)F;
-                    const bool neg = (H >> 31) != 0u;
-                    const uint32_t mb = neg ? 0xCB000000u : 0x4B000000u;
-                    const float mf = neg ? -8388608.0f : 8388608.0f;
-                    f[part][0] = float_of_byte<1>(Fh, mb, mf);
-                    f[part][1] = float_of_byte<0>(Fh, mb, mf);
-                    f[part][2] = float_of_byte<3>(Fl, mb, mf);
-                    f[part][3] = float_of_byte<2>(Fl, mb, mf);
-                    f[part][4] = float_of_byte<1>(Fl, mb, mf);
-                    f[part][5] = float_of_byte<0>(Fl, mb, mf);
+                for (int sl = 0; sl < kOzSlices; sl++) {
+                    float re, im;
+                    tc::up2(tc::sub2(tc::pk2(__uint_as_float(m0[sl]), __uint_as_float(m1[sl])), magic), re, im);
+                    packed[sl][j] = pack_bf16(re, im);
                 }
-#pragma unroll
-                for (int sl = 0; sl < kOzSlices; sl++) packed[sl][j] = pack_bf16(f[0][sl], f[1][sl]);
             }
             const uint32_t off = tc::kmajor_offset(row, half * D + kg * 8, S::KG16, 2);
 #pragma unroll
@@ -242,20 +251,24 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
 #pragma unroll
                 for (int c4 = 0; c4 < 4; c4++) {
                     const int c = ch * 4 + c4;
-                    uint32_t w[4];
+                    // (re, im) of the amplitude as f32x2 pairs
+                    uint64_t a[kOzAccs];
 #pragma unroll
-                    for (int part = 0; part < 2; part++) {
-                        const int j = 2 * c4 + part;
-                        df::f2 t = df::two_sum(acc[0][j], acc[1][j] * 0x1p-8f);
-                        df::f2 t2 = df::two_sum(t.hi, acc[2][j] * 0x1p-16f);
-                        float e = df::add_rn(t.lo, t2.lo);
-                        e = __fmaf_rn(acc[3][j], 0x1p-24f, e);
-                        e = __fmaf_rn(acc[4][j], 0x1p-32f, e);
-                        df::f2 y = df::fast_two_sum(t2.hi, e);
-                        // times 2^(E + e_n - 1038), folded into the exponent field
-                        df::encode_words_scaled(y, (int)E + p.colExp[half * D + 2 * c + part] - 1038,
-                                                &w[2 * part + 1], &w[2 * part]);
-                    }
+                    for (int u = 0; u < kOzAccs; u++) a[u] = tc::pk2(acc[u][2 * c4], acc[u][2 * c4 + 1]);
+                    uint64_t t, tl, t2, t2l, y, yl;
+                    tc::two_sum2(a[0], tc::mul2(a[1], tc::pk2(0x1p-8f, 0x1p-8f)), t, tl);
+                    tc::two_sum2(t, tc::mul2(a[2], tc::pk2(0x1p-16f, 0x1p-16f)), t2, t2l);
+                    uint64_t e = tc::add2(tl, t2l);
+                    e = tc::fma2(a[3], tc::pk2(0x1p-24f, 0x1p-24f), e);
+                    e = tc::fma2(a[4], tc::pk2(0x1p-32f, 0x1p-32f), e);
+                    tc::fast_two_sum2(t2, e, y, yl);
+                    df::f2 yr, yi;
+                    tc::up2(y, yr.hi, yi.hi);
+                    tc::up2(yl, yr.lo, yi.lo);
+                    // times 2^(E + e_n - 1038), folded into the exponent field
+                    uint32_t w[4];
+                    df::encode_words_scaled(yr, (int)E + p.colExp[half * D + 2 * c] - 1038, &w[1], &w[0]);
+                    df::encode_words_scaled(yi, (int)E + p.colExp[half * D + 2 * c + 1] - 1038, &w[3], &w[2]);
                     amps[base + p.off[half * kHalf + c]] = make_uint4(w[0], w[1], w[2], w[3]);
                 }
             }
