@@ -235,4 +235,53 @@ DF_HD f2 neg(f2 a) { return {-a.hi, -a.lo}; }
 // df value times a df constant
 DF_HD f2 mul(f2 a, f2 x) { return acc_result(acc_first(a, x)); }
 
+
+#ifdef __CUDACC__
+// ---- packed float pairs: Blackwell's f32x2 instructions (sm_100 and later) do two
+// lanes of FP32 work per issue slot; every lane rounds to nearest like the scalar
+// operations above, so paired code gives bit-identical results
+__device__ __forceinline__ uint64_t pk2(float a, float b) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void up2(uint64_t r, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r)); }
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+    uint64_t r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
+    uint64_t r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+    uint64_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+// Knuth TwoSum and Dekker FastTwoSum (|a| >= |b|) on pairs
+__device__ __forceinline__ void two_sum2(uint64_t a, uint64_t b, uint64_t& s, uint64_t& e) {
+    s = add2(a, b);
+    const uint64_t bb = sub2(s, a);
+    e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+}
+__device__ __forceinline__ void fast_two_sum2(uint64_t a, uint64_t b, uint64_t& s, uint64_t& e) {
+    s = add2(a, b);
+    e = sub2(b, sub2(s, a));
+}
+
+
+// Contraction: ptxas fuses a mul.rn.f32x2 whose result feeds an add.rn.f32x2 into one
+// FMA (measured on GB300; scalar .rn operations are not fused), so paired code that
+// needs a rounded product before an addition forms it as an FMA with a zero addend.
+__device__ __forceinline__ uint64_t prod2(uint64_t a, uint64_t b) { return fma2(a, b, 0ull); }
+#endif
+
 }  // namespace df

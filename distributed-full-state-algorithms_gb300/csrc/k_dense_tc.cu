@@ -256,6 +256,8 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
 #pragma unroll
                     for (int u = 0; u < kOzAccs; u++) a[u] = tc::pk2(acc[u][2 * c4], acc[u][2 * c4 + 1]);
                     uint64_t t, tl, t2, t2l, y, yl;
+                    // products by powers of two are exact, so ptxas may fuse them into the
+                    // additions that follow without changing a bit
                     tc::two_sum2(a[0], tc::mul2(a[1], tc::pk2(0x1p-8f, 0x1p-8f)), t, tl);
                     tc::two_sum2(t, tc::mul2(a[2], tc::pk2(0x1p-16f, 0x1p-16f)), t2, t2l);
                     uint64_t e = tc::add2(tl, t2l);

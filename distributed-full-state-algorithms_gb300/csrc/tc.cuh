@@ -97,44 +97,15 @@ DEV void ld8(uint32_t taddr, float (&v)[16]) {
 }
 DEV void ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// ---- packed float pairs: Blackwell's f32x2 instructions do two lanes of FP32 work
-// per issue slot (round to nearest, no contraction)
-DEV uint64_t pk2(float a, float b) {
-    uint64_t r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-DEV void up2(uint64_t r, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r)); }
-DEV uint64_t add2(uint64_t a, uint64_t b) {
-    uint64_t r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-DEV uint64_t sub2(uint64_t a, uint64_t b) {
-    uint64_t r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-DEV uint64_t mul2(uint64_t a, uint64_t b) {
-    uint64_t r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-DEV uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
-    uint64_t r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-// Knuth TwoSum and Dekker FastTwoSum (|a| >= |b|) on pairs
-DEV void two_sum2(uint64_t a, uint64_t b, uint64_t& s, uint64_t& e) {
-    s = add2(a, b);
-    const uint64_t bb = sub2(s, a);
-    e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
-}
-DEV void fast_two_sum2(uint64_t a, uint64_t b, uint64_t& s, uint64_t& e) {
-    s = add2(a, b);
-    e = sub2(b, sub2(s, a));
-}
+// packed float pairs (df::pk2 ...) for the epilogues
+using df::add2;
+using df::fast_two_sum2;
+using df::fma2;
+using df::mul2;
+using df::pk2;
+using df::sub2;
+using df::two_sum2;
+using df::up2;
 
 // byte offset of element (row, k) of a K-major operand with `kgroups` core
 // matrices along K per 8-row block (16-byte core rows, `esize`-byte elements)
