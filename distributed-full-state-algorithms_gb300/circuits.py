@@ -328,11 +328,12 @@ def algorithmic_bytes(g: Gate, num_amps: int, elem_bytes: int) -> int:
         return num_amps * elem_bytes
     if g.kind == "deph1":
         return num_amps * elem_bytes
-    if g.kind == "dm_many_targ":
-        return 2 * full
+    if g.kind == "dm_many_targ" and len(g.qubits) > 2:
+        return 2 * full  # U on the ket qubits, then conj(U) on the bra qubits
     return full
 
 
 def kernel_launches(g: Gate) -> int:
     """Engine kernel launches issued for one gate."""
-    return 2 if g.kind == "dm_many_targ" else 1
+    # a density-matrix gate on k <= 2 targets is one superoperator sweep on 2k targets
+    return 2 if g.kind == "dm_many_targ" and len(g.qubits) > 2 else 1

@@ -430,8 +430,25 @@ int dfs_densitymatrix_manyTargGate(dfs_state s, const unsigned* targets, unsigne
     if (!rc) rc = check_list(targets, k, s->numQubits, "target", false);
     if (!rc && !gate) rc = fail(DFS_ERR_INVALID_ARG, "null gate");
     if (rc) return rc;
-    if ((rc = sv_many_targ(s, targets, k, gate))) return rc;
     size_t d = (size_t)1 << k;
+    if (k <= 2 && s->precision != DFS_C128_NATIVE) {
+        // one sweep of the superoperator U (x) conj(U) on targets ++ targets+n (the
+        // layout of getSuperoperator, src/misc.hpp:58-81): local index a + d*b with ket
+        // bits a and bra bits b, S[a + d b][a' + d b'] = U[a][a'] conj(U[b][b']).  At
+        // 2k = 4 targets it runs on the tensor cores; either way it halves the sweeps.
+        const size_t sd = d * d;
+        const std::complex<double>* U = reinterpret_cast<const std::complex<double>*>(gate);
+        std::vector<std::complex<double>> S(sd * sd);
+        for (size_t b = 0; b < d; b++)
+            for (size_t a = 0; a < d; a++)
+                for (size_t bp = 0; bp < d; bp++)
+                    for (size_t ap = 0; ap < d; ap++)
+                        S[(a + d * b) * sd + (ap + d * bp)] = U[a * d + ap] * std::conj(U[b * d + bp]);
+        std::vector<unsigned> ext(targets, targets + k);
+        for (unsigned i = 0; i < k; i++) ext.push_back(targets[i] + s->numQubits);
+        return sv_many_targ(s, ext.data(), 2 * k, reinterpret_cast<const double*>(S.data()));
+    }
+    if ((rc = sv_many_targ(s, targets, k, gate))) return rc;
     std::vector<double> conjGate(gate, gate + 2 * d * d);
     for (size_t e = 0; e < d * d; e++) conjGate[2 * e + 1] = -conjGate[2 * e + 1];
     std::vector<unsigned> bra = shifted(targets, k, s->numQubits);
