@@ -59,6 +59,10 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the e2e, FP32 and native-FP64 legs")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the adjoint, batched and 32-qubit precision legs")
+    ap.add_argument("--legs", default="adjoint,batched,precision32",
+                    help="comma-separated forms to run (adjoint, batched, precision32)")
+    ap.add_argument("--form-scale", default="full", choices=["full", "small"],
+                    help="small: the forms at reduced sizes, for profiling captures")
     return ap.parse_args()
 
 
@@ -417,9 +421,13 @@ def gpu_arm(args, world, rank, local):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args, circuits, gates)
     if not args.no_forms:
-        for name, leg in (("adjoint", adjoint_leg), ("batched", batch_leg), ("precision32", precision_leg)):
+        legs = {"adjoint": adjoint_leg, "batched": batch_leg, "precision32": precision_leg}
+        for name in [x for x in args.legs.split(",") if x]:
+            if name not in legs:
+                result[name] = {"error": "unknown leg"}
+                continue
             try:
-                result[name] = leg(dfs, circuits)
+                result[name] = legs[name](dfs, circuits, small=args.form_scale == "small")
             except Exception as e:  # a failing extra leg must not lose the headline line
                 result[name] = {"error": f"{type(e).__name__}: {e}"}
     return result, rank
@@ -435,9 +443,9 @@ def _sync_time(dfs, fn):
     return (time.perf_counter() - t0) * 1e3, out
 
 
-def adjoint_leg(dfs, circuits):
+def adjoint_leg(dfs, circuits, small=False):
     """Full adjoint gradient against one forward pass (same <H>), complex128 and complex64."""
-    n = ADJ_QUBITS
+    n = ADJ_QUBITS  # already a few-GB case (two 256 MiB vectors)
     gates = circuits.gadget_ansatz(n, ADJ_LAYERS, ADJ_PER_LAYER, seed=CIRCUIT_SEED)
     coeffs, paulis = circuits.pauli_sum(n, ADJ_TERMS, seed=7)
     circ, params = circuits.record(dfs, n, gates)
@@ -482,14 +490,15 @@ def batch_bytes(specs, circuits, elem):
     return total
 
 
-def batch_leg(dfs, circuits):
+def batch_leg(dfs, circuits, small=False):
     """One persistent launch (graph replay) for every circuit's <H> and gradient, against
     per-circuit runs through the circuit runtime."""
-    specs = circuits.batch_mix(BATCH_CIRCUITS, BATCH_MIN_Q, BATCH_MAX_Q, BATCH_GATES, BATCH_TERMS, BATCH_SEED)
+    specs = circuits.batch_mix(128 if small else BATCH_CIRCUITS, BATCH_MIN_Q, BATCH_MAX_Q, BATCH_GATES, BATCH_TERMS,
+                               BATCH_SEED)
     recs = [circuits.record(dfs, n, g, parametrise=("pauli_gadget", "phase_gadget")) for n, g, _, _ in specs]
     circs = [r[0] for r in recs]
     params = [r[1] for r in recs]
-    out = {"workload": f"{BATCH_CIRCUITS} statevector circuits of {BATCH_MIN_Q}-{BATCH_MAX_Q} qubits, "
+    out = {"workload": f"{len(specs)} statevector circuits of {BATCH_MIN_Q}-{max(x[0] for x in specs)} qubits, "
                        f"{BATCH_GATES} gates each, H of {BATCH_TERMS} terms, <H> and adjoint gradient per circuit",
            "total_amplitudes": int(sum(1 << s[0] for s in specs))}
     for prec, elem in (("c128", 16), ("c64", 8)):
@@ -528,10 +537,10 @@ def batch_leg(dfs, circuits):
     return out
 
 
-def precision_leg(dfs, circuits):
+def precision_leg(dfs, circuits, small=False):
     """complex64 against complex128 at 32 qubits: time, <H> error and fidelity; the
     complex128 engine (parity-pinned to the oracle) stands for the FP64 reference."""
-    n = PREC_QUBITS
+    n = 26 if small else PREC_QUBITS
     gates = circuits.gate_mix(n, NUM_GATES, CIRCUIT_SEED, dense_k=PREC_DENSE)
     coeffs, paulis = circuits.pauli_sum(n, PREC_TERMS, seed=7)
     res = {"workload": f"sv{n} gate mix + dense k={list(PREC_DENSE)}, {NUM_GATES} gates, H of {PREC_TERMS} terms"}
