@@ -283,6 +283,217 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
     if (warp == 0) tc::tmem_free<S::COLS64>(tmem);
 }
 
+// ------------------------------------------- complex128, warp-specialised (k = 3)
+// The same arithmetic as k_dense_ozaki, with the phases of consecutive tiles overlapped
+// instead of separated by CTA barriers: four slicer warps (one group per thread, so the
+// group's exponent needs no exchange) fill one of two shared-memory A buffers, one thread
+// issues the MMAs of a full buffer into one of two TMEM accumulator sets, and four
+// epilogue warps drain the other set.  Per buffer b, mbarriers carry the hand-offs:
+//   fullA[b]   slicers -> MMA issuer   (A[b] written, count 128)
+//   issued[b]  MMA issuer -> epilogue  (MMAs issued; carries the slicers' exponents)
+//   mmaDone[b] tensor cores -> epilogue (tcgen05.commit)
+//   accFree[b] epilogue -> slicers, MMA issuer (accumulators read, so A[b] is free too)
+// Tile i uses buffer i & 1 for the (i >> 1)-th time; every wait names the parity of the
+// phase it needs, and no barrier can run two phases ahead of a waiter (each next phase
+// depends on that waiter's own later arrival).  Every wait is bounded.
+constexpr int kWsRole = 128;                  // threads per slicer / epilogue role
+constexpr int kWsThreads = 2 * kWsRole + 32;  // + one warp for the MMA issuer
+constexpr uint32_t kWsAccCols = 128;          // per accumulator set (5 x 16 used)
+
+template <class IT>
+__global__ void __launch_bounds__(kWsThreads, 2) k_dense_ozaki_ws(uint4* __restrict__ amps, IT numGroups,
+                                                                  DenseParams<IT, 3> p, const uint4* __restrict__ bsl) {
+    using S = Dense<3>;
+    constexpr int D = S::D, R = S::R;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* sB = smem + 2 * kOzSlices * S::A16;
+    __shared__ __align__(8) uint64_t fullA[2], issued[2], mmaDone[2], accFree[2], drain;
+    __shared__ uint32_t tmemSlot;
+    __shared__ uint32_t sE[2][128];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    for (int i = tid; i < (int)(kOzBCopies * kOzSlices * S::B16 / 16); i += kWsThreads)
+        reinterpret_cast<uint4*>(sB)[i] = bsl[i];
+    if (warp == 0) tc::tmem_alloc<2 * kWsAccCols>(&tmemSlot);
+    if (tid == 0) {
+        for (int b = 0; b < 2; b++) {
+            tc::mbar_init(&fullA[b], kWsRole);
+            tc::mbar_init(&issued[b], 1);
+            tc::mbar_init(&mmaDone[b], 1);
+            tc::mbar_init(&accFree[b], kWsRole);
+        }
+        tc::mbar_init(&drain, 1);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tmemSlot;
+    const IT numTiles = (numGroups + 127) / 128;
+    const int myTiles = (IT)blockIdx.x < numTiles ? (int)((numTiles - 1 - (IT)blockIdx.x) / gridDim.x) + 1 : 0;
+    bool ok = true;
+
+    if (warp < 4) {
+        // ---- slicers: thread `tid` slices group `tid` of each tile
+        const int row = tid;
+        auto load = [&](int i, uint4 (&v)[D]) {
+            const IT g = ((IT)blockIdx.x + (IT)i * gridDim.x) * 128 + (IT)row;
+            const bool in = i < myTiles && g < numGroups;
+            const IT b = in ? insert_zeros(g, p.q) : (IT)0;
+#pragma unroll
+            for (int c = 0; c < D; c++) v[c] = in ? amps[b + p.off[c]] : make_uint4(0, 0, 0, 0);
+        };
+        uint4 cur[D], nxt[D];
+        load(0, cur);
+        for (int i = 0; i < myTiles; i++) {
+            const int b = i & 1;
+            const uint32_t k = (uint32_t)i >> 1;
+            if (i >= 2 && !(ok = tc::mbar_wait(&accFree[b], (k - 1) & 1, kTcWaitLimit))) break;
+            uint32_t E = 0;
+#pragma unroll
+            for (int c = 0; c < D; c++) E = max(E, max((cur[c].y >> 20) & 0x7FFu, (cur[c].w >> 20) & 0x7FFu));
+            sE[b][row] = E;
+            unsigned char* sA = smem + b * kOzSlices * S::A16;
+#pragma unroll
+            for (int kg = 0; kg < D / 4; kg++) {
+                uint32_t packed[kOzSlices][4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const uint4 v = cur[kg * 4 + j];
+                    const uint64_t F0 = fraction48(v.y, v.x, E), F1 = fraction48(v.w, v.z, E);
+                    const uint32_t Fh0 = (uint32_t)(F0 >> 32), Fl0 = (uint32_t)F0;
+                    const uint32_t Fh1 = (uint32_t)(F1 >> 32), Fl1 = (uint32_t)F1;
+                    const uint32_t mb0 = (v.y >> 31) ? 0xCB000000u : 0x4B000000u;
+                    const uint32_t mb1 = (v.w >> 31) ? 0xCB000000u : 0x4B000000u;
+                    const uint64_t magic = tc::pk2(__uint_as_float(mb0), __uint_as_float(mb1));
+                    uint32_t m0[kOzSlices], m1[kOzSlices];
+                    m0[0] = __byte_perm(Fh0, mb0, 0x7651u);
+                    m0[1] = __byte_perm(Fh0, mb0, 0x7650u);
+                    m0[2] = __byte_perm(Fl0, mb0, 0x7653u);
+                    m0[3] = __byte_perm(Fl0, mb0, 0x7652u);
+                    m0[4] = __byte_perm(Fl0, mb0, 0x7651u);
+                    m0[5] = __byte_perm(Fl0, mb0, 0x7650u);
+                    m1[0] = __byte_perm(Fh1, mb1, 0x7651u);
+                    m1[1] = __byte_perm(Fh1, mb1, 0x7650u);
+                    m1[2] = __byte_perm(Fl1, mb1, 0x7653u);
+                    m1[3] = __byte_perm(Fl1, mb1, 0x7652u);
+                    m1[4] = __byte_perm(Fl1, mb1, 0x7651u);
+                    m1[5] = __byte_perm(Fl1, mb1, 0x7650u);
+#pragma unroll
+                    for (int sl = 0; sl < kOzSlices; sl++) {
+                        float re, im;
+                        tc::up2(tc::sub2(tc::pk2(__uint_as_float(m0[sl]), __uint_as_float(m1[sl])), magic), re, im);
+                        packed[sl][j] = pack_bf16(re, im);
+                    }
+                }
+                const uint32_t off = tc::kmajor_offset(row, kg * 8, S::KG16, 2);
+#pragma unroll
+                for (int sl = 0; sl < kOzSlices; sl++)
+                    *reinterpret_cast<uint4*>(sA + sl * S::A16 + off) =
+                        make_uint4(packed[sl][0], packed[sl][1], packed[sl][2], packed[sl][3]);
+            }
+            load(i + 1, nxt);
+            tc::fence_smem_to_async();
+            tc::mbar_arrive(&fullA[b]);
+#pragma unroll
+            for (int c = 0; c < D; c++) cur[c] = nxt[c];
+        }
+    } else if (warp < 8) {
+        // ---- epilogue: thread reads TMEM lane `row` (its warp's quadrant) and writes group `row`
+        const int row = tid - kWsRole;
+        for (int i = 0; i < myTiles; i++) {
+            const int b = i & 1;
+            const uint32_t k = (uint32_t)i >> 1;
+            if (!(ok = tc::mbar_wait(&issued[b], k & 1, kTcWaitLimit) && tc::mbar_wait(&mmaDone[b], k & 1, kTcWaitLimit)))
+                break;
+            tc::fence_after_sync();
+            const uint32_t E = sE[b][row];
+            const IT g = ((IT)blockIdx.x + (IT)i * gridDim.x) * 128 + (IT)row;
+            const bool valid = g < numGroups;
+            const IT base = valid ? insert_zeros(g, p.q) : (IT)0;
+            const uint32_t lanes = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)b * kWsAccCols;
+#pragma unroll
+            for (int ch = 0; ch < D / 4; ch++) {
+                float acc[kOzAccs][8];
+#pragma unroll
+                for (int u = 0; u < kOzAccs; u++) {
+                    float v[16];
+                    tc::ld8(lanes + (uint32_t)(u * R + ch * 8), v);
+#pragma unroll
+                    for (int j = 0; j < 8; j++) acc[u][j] = v[j];
+                }
+                tc::ld_wait();
+                if (valid) {
+#pragma unroll
+                    for (int c4 = 0; c4 < 4; c4++) {
+                        const int c = ch * 4 + c4;
+                        uint64_t a[kOzAccs];
+#pragma unroll
+                        for (int u = 0; u < kOzAccs; u++) a[u] = tc::pk2(acc[u][2 * c4], acc[u][2 * c4 + 1]);
+                        uint64_t t, tl, t2, t2l, y, yl;
+                        tc::two_sum2(a[0], tc::mul2(a[1], tc::pk2(0x1p-8f, 0x1p-8f)), t, tl);
+                        tc::two_sum2(t, tc::mul2(a[2], tc::pk2(0x1p-16f, 0x1p-16f)), t2, t2l);
+                        uint64_t e = tc::add2(tl, t2l);
+                        e = tc::fma2(a[3], tc::pk2(0x1p-24f, 0x1p-24f), e);
+                        e = tc::fma2(a[4], tc::pk2(0x1p-32f, 0x1p-32f), e);
+                        tc::fast_two_sum2(t2, e, y, yl);
+                        df::f2 yr, yi;
+                        tc::up2(y, yr.hi, yi.hi);
+                        tc::up2(yl, yr.lo, yi.lo);
+                        uint32_t w[4];
+                        df::encode_words_scaled(yr, (int)E + p.colExp[2 * c] - 1038, &w[1], &w[0]);
+                        df::encode_words_scaled(yi, (int)E + p.colExp[2 * c + 1] - 1038, &w[3], &w[2]);
+                        amps[base + p.off[c]] = make_uint4(w[0], w[1], w[2], w[3]);
+                    }
+                }
+            }
+            tc::fence_before_sync();
+            tc::mbar_arrive(&accFree[b]);
+        }
+    } else if (lane == 0) {
+        // ---- MMA issuer: the 21 slice products of weight 2^-8u (u = s + t <= 5)
+        const uint32_t id = tc::idesc(1, R);
+        int issuedTiles = 0;
+        for (int i = 0; i < myTiles; i++) {
+            const int b = i & 1;
+            const uint32_t k = (uint32_t)i >> 1;
+            if (!(ok = tc::mbar_wait(&fullA[b], k & 1, kTcWaitLimit))) break;
+            if (i >= 2 && !(ok = tc::mbar_wait(&accFree[b], (k - 1) & 1, kTcWaitLimit))) break;
+            tc::fence_after_sync();
+            const unsigned char* sA = smem + b * kOzSlices * S::A16;
+            const uint32_t dst = tmem + (uint32_t)b * kWsAccCols;
+#pragma unroll
+            for (int u = 0; u < kOzSlices; u++) {
+                const int acc = u < kOzAccs ? u : kOzAccs - 1;
+                const int copy = u < kOzAccs ? 0 : u - (kOzAccs - 1);
+#pragma unroll
+                for (int sl = 0; sl <= u; sl++) {
+                    const int t = u - sl;
+#pragma unroll
+                    for (int ks = 0; ks < R / 16; ks++) {
+                        uint64_t da = tc::desc(tc::smem_u32(sA + sl * S::A16 + ks * 256), 128, 128 * S::KG16);
+                        uint64_t db = tc::desc(
+                            tc::smem_u32(sB + (copy * kOzSlices + t) * S::B16 + ks * 256), 128, 128 * S::KG16);
+                        const bool first = u <= kOzAccs - 1 && sl == 0 && ks == 0;
+                        tc::mma_bf16(dst + (uint32_t)(acc * R), da, db, id, first ? 0u : 1u);
+                    }
+                }
+            }
+            tc::commit(&mmaDone[b]);
+            tc::mbar_arrive(&issued[b]);
+            issuedTiles++;
+        }
+        // every issued MMA has completed before TMEM is released
+        if (issuedTiles > 0) {
+            tc::commit(&drain);
+            if (!tc::mbar_wait(&drain, 0, kTcWaitLimit)) ok = false;
+        }
+    }
+    if (!ok) atomicExch(&g_tcTimeout, 1);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_free<2 * kWsAccCols>(tmem);
+}
+
 // ------------------------------------------------------------- complex64
 
 DEV uint32_t to_tf32(float x) {
@@ -531,6 +742,16 @@ static int dense_tc_run(State* s, const unsigned* targs, const double* g) {
         auto kern = k_dense_3xtf32<IT, KT>;
         if ((rc = set_smem(kern, smem))) return rc;
         kern<<<grid, kTcThreads, smem, ctx().stream>>>((float2*)s->amps, groups, p, (const uint4*)ctx().scratch);
+    } else if constexpr (KT == 3) {
+        // warp-specialised: two A buffers and two accumulator sets (256 TMEM columns) per CTA;
+        // shared memory padded so that no third CTA can join an SM's 512 columns
+        const size_t perSMws = ctx().smemOptin + 1024;
+        const size_t wsSmem = std::max<size_t>(2 * kOzSlices * S::A16 + kOzBCopies * kOzSlices * S::B16,
+                                               std::min<size_t>(perSMws / 3 + 1, perSMws / 2 - 3 * 1024));
+        auto kern = k_dense_ozaki_ws<IT>;
+        if ((rc = set_smem(kern, wsSmem))) return rc;
+        const unsigned wsGrid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(tiles, (uint64_t)ctx().numSMs * 2));
+        kern<<<wsGrid, kWsThreads, wsSmem, ctx().stream>>>((uint4*)s->amps, groups, p, (const uint4*)ctx().scratch);
     } else if constexpr (S::kOzakiFits) {
         auto kern = k_dense_ozaki<IT, KT>;
         if ((rc = set_smem(kern, smem))) return rc;
