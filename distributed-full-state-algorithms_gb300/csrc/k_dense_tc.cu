@@ -288,16 +288,18 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
 // instead of separated by CTA barriers: four slicer warps (one group per thread, so the
 // group's exponent needs no exchange) fill one of two shared-memory A buffers, one thread
 // issues the MMAs of a full buffer into one of two TMEM accumulator sets, and four
-// epilogue warps drain the other set.  Per buffer b, mbarriers carry the hand-offs:
-//   fullA[b]   slicers -> MMA issuer   (A[b] written, count 128)
+// epilogue warps drain the other set.  Two slicer threads share a group (adjacent lanes,
+// so the group's exponent is one shuffle away), each slicing half of its amplitudes.  Per buffer b, mbarriers carry the hand-offs:
+//   fullA[b]   slicers -> MMA issuer   (A[b] written, count 256)
 //   issued[b]  MMA issuer -> epilogue  (MMAs issued; carries the slicers' exponents)
 //   mmaDone[b] tensor cores -> epilogue (tcgen05.commit)
 //   accFree[b] epilogue -> slicers, MMA issuer (accumulators read, so A[b] is free too)
 // Tile i uses buffer i & 1 for the (i >> 1)-th time; every wait names the parity of the
 // phase it needs, and no barrier can run two phases ahead of a waiter (each next phase
 // depends on that waiter's own later arrival).  Every wait is bounded.
-constexpr int kWsRole = 128;                  // threads per slicer / epilogue role
-constexpr int kWsThreads = 2 * kWsRole + 32;  // + one warp for the MMA issuer
+constexpr int kWsRole = 128;                          // epilogue threads: one per group of a tile
+constexpr int kWsSlicers = 256;                       // two slicer threads per group
+constexpr int kWsThreads = kWsSlicers + kWsRole + 32;  // + one warp for the MMA issuer
 constexpr uint32_t kWsAccCols = 128;          // per accumulator set (5 x 16 used)
 
 template <class IT>
@@ -317,7 +319,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_dense_ozaki_ws(uint4* __restr
     if (warp == 0) tc::tmem_alloc<2 * kWsAccCols>(&tmemSlot);
     if (tid == 0) {
         for (int b = 0; b < 2; b++) {
-            tc::mbar_init(&fullA[b], kWsRole);
+            tc::mbar_init(&fullA[b], kWsSlicers);
             tc::mbar_init(&issued[b], 1);
             tc::mbar_init(&mmaDone[b], 1);
             tc::mbar_init(&accFree[b], kWsRole);
@@ -332,17 +334,18 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_dense_ozaki_ws(uint4* __restr
     const int myTiles = (IT)blockIdx.x < numTiles ? (int)((numTiles - 1 - (IT)blockIdx.x) / gridDim.x) + 1 : 0;
     bool ok = true;
 
-    if (warp < 4) {
-        // ---- slicers: thread `tid` slices group `tid` of each tile
-        const int row = tid;
-        auto load = [&](int i, uint4 (&v)[D]) {
+    if (tid < kWsSlicers) {
+        // ---- slicers: threads 2r and 2r+1 slice halves 0 and 1 of group r of each tile
+        constexpr int H = D / 2;  // amplitudes per slicer thread
+        const int row = tid >> 1, half = tid & 1;
+        auto load = [&](int i, uint4 (&v)[H]) {
             const IT g = ((IT)blockIdx.x + (IT)i * gridDim.x) * 128 + (IT)row;
             const bool in = i < myTiles && g < numGroups;
             const IT b = in ? insert_zeros(g, p.q) : (IT)0;
 #pragma unroll
-            for (int c = 0; c < D; c++) v[c] = in ? amps[b + p.off[c]] : make_uint4(0, 0, 0, 0);
+            for (int c = 0; c < H; c++) v[c] = in ? amps[b + p.off[half * H + c]] : make_uint4(0, 0, 0, 0);
         };
-        uint4 cur[D], nxt[D];
+        uint4 cur[H], nxt[H];
         load(0, cur);
         for (int i = 0; i < myTiles; i++) {
             const int b = i & 1;
@@ -350,15 +353,15 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_dense_ozaki_ws(uint4* __restr
             if (i >= 2 && !(ok = tc::mbar_wait(&accFree[b], (k - 1) & 1, kTcWaitLimit))) break;
             uint32_t E = 0;
 #pragma unroll
-            for (int c = 0; c < D; c++) E = max(E, max((cur[c].y >> 20) & 0x7FFu, (cur[c].w >> 20) & 0x7FFu));
-            sE[b][row] = E;
+            for (int c = 0; c < H; c++) E = max(E, max((cur[c].y >> 20) & 0x7FFu, (cur[c].w >> 20) & 0x7FFu));
+            E = max(E, __shfl_xor_sync(0xffffffffu, E, 1));
+            if (half == 0) sE[b][row] = E;
             unsigned char* sA = smem + b * kOzSlices * S::A16;
-#pragma unroll
-            for (int kg = 0; kg < D / 4; kg++) {
+            {
                 uint32_t packed[kOzSlices][4];
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
-                    const uint4 v = cur[kg * 4 + j];
+                    const uint4 v = cur[j];
                     const uint64_t F0 = fraction48(v.y, v.x, E), F1 = fraction48(v.w, v.z, E);
                     const uint32_t Fh0 = (uint32_t)(F0 >> 32), Fl0 = (uint32_t)F0;
                     const uint32_t Fh1 = (uint32_t)(F1 >> 32), Fl1 = (uint32_t)F1;
@@ -385,7 +388,8 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_dense_ozaki_ws(uint4* __restr
                         packed[sl][j] = pack_bf16(re, im);
                     }
                 }
-                const uint32_t off = tc::kmajor_offset(row, kg * 8, S::KG16, 2);
+                // this half's 8 reals are one 16-byte core row per slice
+                const uint32_t off = tc::kmajor_offset(row, half * 8, S::KG16, 2);
 #pragma unroll
                 for (int sl = 0; sl < kOzSlices; sl++)
                     *reinterpret_cast<uint4*>(sA + sl * S::A16 + off) =
@@ -395,11 +399,11 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_dense_ozaki_ws(uint4* __restr
             tc::fence_smem_to_async();
             tc::mbar_arrive(&fullA[b]);
 #pragma unroll
-            for (int c = 0; c < D; c++) cur[c] = nxt[c];
+            for (int c = 0; c < H; c++) cur[c] = nxt[c];
         }
-    } else if (warp < 8) {
+    } else if (tid < kWsSlicers + kWsRole) {
         // ---- epilogue: thread reads TMEM lane `row` (its warp's quadrant) and writes group `row`
-        const int row = tid - kWsRole;
+        const int row = tid - kWsSlicers;
         for (int i = 0; i < myTiles; i++) {
             const int b = i & 1;
             const uint32_t k = (uint32_t)i >> 1;
