@@ -283,30 +283,43 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
     if (warp == 0) tc::tmem_free<S::COLS64>(tmem);
 }
 
-// ------------------------------------------- complex128, warp-specialised (k = 3)
+// ------------------------------------------ complex128, warp-specialised (k = 3)
 // The same arithmetic as k_dense_ozaki, with the phases of consecutive tiles overlapped
-// instead of separated by CTA barriers: four slicer warps (one group per thread, so the
-// group's exponent needs no exchange) fill one of two shared-memory A buffers, one thread
-// issues the MMAs of a full buffer into one of two TMEM accumulator sets, and four
-// epilogue warps drain the other set.  Two slicer threads share a group (adjacent lanes,
-// so the group's exponent is one shuffle away), each slicing half of its amplitudes.  Per buffer b, mbarriers carry the hand-offs:
-//   fullA[b]   slicers -> MMA issuer   (A[b] written, count 256)
+// instead of separated by CTA barriers: slicer warps fill one of two shared-memory A
+// buffers, one thread issues the MMAs of a full buffer into one of two TMEM accumulator
+// sets, and epilogue warps drain the other set.  The SPR slicer threads of a group are
+// adjacent lanes, so the group's exponent is a shuffle away; each slices 4 amplitudes
+// (one 16-byte core row per slice).  Per buffer b, mbarriers carry the hand-offs:
+//   fullA[b]   slicers -> MMA issuer   (A[b] written, one arrival per slicer thread)
 //   issued[b]  MMA issuer -> epilogue  (MMAs issued; carries the slicers' exponents)
 //   mmaDone[b] tensor cores -> epilogue (tcgen05.commit)
 //   accFree[b] epilogue -> slicers, MMA issuer (accumulators read, so A[b] is free too)
 // Tile i uses buffer i & 1 for the (i >> 1)-th time; every wait names the parity of the
 // phase it needs, and no barrier can run two phases ahead of a waiter (each next phase
 // depends on that waiter's own later arrival).  Every wait is bounded.
-constexpr int kWsRole = 128;                          // epilogue threads: one per group of a tile
-constexpr int kWsSlicers = 256;                       // two slicer threads per group
-constexpr int kWsThreads = kWsSlicers + kWsRole + 32;  // + one warp for the MMA issuer
-constexpr uint32_t kWsAccCols = 128;          // per accumulator set (5 x 16 used)
+// Shapes per target count: SPR slicer threads per group (4 amplitudes each), EPQ epilogue
+// warps per TMEM lane quadrant, the columns of one accumulator set, CTAs per SM.  Only
+// k = 3 uses it: at k = 4 (SPR 4, EPQ 2, one CTA per SM for the 512 TMEM columns of two
+// accumulator sets) it measured 11.8 ms at 30 qubits against 9.9 for k_dense_ozaki.
+template <int KT>
+struct WsShape;
+template <>
+struct WsShape<3> {
+    static constexpr int SPR = 2, EPQ = 1, kMinBlocks = 2;
+    static constexpr uint32_t kAccCols = 128;  // 5 x 16 used
+};
+template <int KT>
+constexpr int ws_threads() {
+    return 128 * WsShape<KT>::SPR + 128 * WsShape<KT>::EPQ + 32;  // + one warp for the MMA issuer
+}
 
-template <class IT>
-__global__ void __launch_bounds__(kWsThreads, 2) k_dense_ozaki_ws(uint4* __restrict__ amps, IT numGroups,
-                                                                  DenseParams<IT, 3> p, const uint4* __restrict__ bsl) {
-    using S = Dense<3>;
+template <class IT, int KT>
+__global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
+    k_dense_ozaki_ws(uint4* __restrict__ amps, IT numGroups, DenseParams<IT, KT> p, const uint4* __restrict__ bsl) {
+    using S = Dense<KT>;
+    using W = WsShape<KT>;
     constexpr int D = S::D, R = S::R;
+    constexpr int kSlicers = 128 * W::SPR, kEpi = 128 * W::EPQ, kThreadsAll = ws_threads<KT>();
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* sB = smem + 2 * kOzSlices * S::A16;
     __shared__ __align__(8) uint64_t fullA[2], issued[2], mmaDone[2], accFree[2], drain;
@@ -314,15 +327,15 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_dense_ozaki_ws(uint4* __restr
     __shared__ uint32_t sE[2][128];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    for (int i = tid; i < (int)(kOzBCopies * kOzSlices * S::B16 / 16); i += kWsThreads)
+    for (int i = tid; i < (int)(kOzBCopies * kOzSlices * S::B16 / 16); i += kThreadsAll)
         reinterpret_cast<uint4*>(sB)[i] = bsl[i];
-    if (warp == 0) tc::tmem_alloc<2 * kWsAccCols>(&tmemSlot);
+    if (warp == 0) tc::tmem_alloc<2 * W::kAccCols>(&tmemSlot);
     if (tid == 0) {
         for (int b = 0; b < 2; b++) {
-            tc::mbar_init(&fullA[b], kWsSlicers);
+            tc::mbar_init(&fullA[b], kSlicers);
             tc::mbar_init(&issued[b], 1);
             tc::mbar_init(&mmaDone[b], 1);
-            tc::mbar_init(&accFree[b], kWsRole);
+            tc::mbar_init(&accFree[b], kEpi);
         }
         tc::mbar_init(&drain, 1);
     }
@@ -334,16 +347,16 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_dense_ozaki_ws(uint4* __restr
     const int myTiles = (IT)blockIdx.x < numTiles ? (int)((numTiles - 1 - (IT)blockIdx.x) / gridDim.x) + 1 : 0;
     bool ok = true;
 
-    if (tid < kWsSlicers) {
-        // ---- slicers: threads 2r and 2r+1 slice halves 0 and 1 of group r of each tile
-        constexpr int H = D / 2;  // amplitudes per slicer thread
-        const int row = tid >> 1, half = tid & 1;
+    if (tid < kSlicers) {
+        // ---- slicers: the SPR adjacent threads of group r slice its amplitudes 4 at a time
+        constexpr int H = 4;
+        const int row = tid / W::SPR, part = tid % W::SPR;
         auto load = [&](int i, uint4 (&v)[H]) {
             const IT g = ((IT)blockIdx.x + (IT)i * gridDim.x) * 128 + (IT)row;
             const bool in = i < myTiles && g < numGroups;
             const IT b = in ? insert_zeros(g, p.q) : (IT)0;
 #pragma unroll
-            for (int c = 0; c < H; c++) v[c] = in ? amps[b + p.off[half * H + c]] : make_uint4(0, 0, 0, 0);
+            for (int c = 0; c < H; c++) v[c] = in ? amps[b + p.off[part * H + c]] : make_uint4(0, 0, 0, 0);
         };
         uint4 cur[H], nxt[H];
         load(0, cur);
@@ -354,8 +367,9 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_dense_ozaki_ws(uint4* __restr
             uint32_t E = 0;
 #pragma unroll
             for (int c = 0; c < H; c++) E = max(E, max((cur[c].y >> 20) & 0x7FFu, (cur[c].w >> 20) & 0x7FFu));
-            E = max(E, __shfl_xor_sync(0xffffffffu, E, 1));
-            if (half == 0) sE[b][row] = E;
+#pragma unroll
+            for (int m = 1; m < W::SPR; m <<= 1) E = max(E, __shfl_xor_sync(0xffffffffu, E, m));
+            if (part == 0) sE[b][row] = E;
             unsigned char* sA = smem + b * kOzSlices * S::A16;
             {
                 uint32_t packed[kOzSlices][4];
@@ -388,8 +402,8 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_dense_ozaki_ws(uint4* __restr
                         packed[sl][j] = pack_bf16(re, im);
                     }
                 }
-                // this half's 8 reals are one 16-byte core row per slice
-                const uint32_t off = tc::kmajor_offset(row, half * 8, S::KG16, 2);
+                // this thread's 8 reals are one 16-byte core row per slice
+                const uint32_t off = tc::kmajor_offset(row, part * 8, S::KG16, 2);
 #pragma unroll
                 for (int sl = 0; sl < kOzSlices; sl++)
                     *reinterpret_cast<uint4*>(sA + sl * S::A16 + off) =
@@ -401,9 +415,11 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_dense_ozaki_ws(uint4* __restr
 #pragma unroll
             for (int c = 0; c < H; c++) cur[c] = nxt[c];
         }
-    } else if (tid < kWsSlicers + kWsRole) {
-        // ---- epilogue: thread reads TMEM lane `row` (its warp's quadrant) and writes group `row`
-        const int row = tid - kWsSlicers;
+    } else if (tid < kSlicers + kEpi) {
+        // ---- epilogue: warp ew reads TMEM lane quadrant ew & 3 (the epilogue starts at a
+        //      multiple of four warps) and drains chunks of 4 amplitudes ew >> 2, + EPQ, ...
+        const int ew = warp - kSlicers / 32, cg = ew >> 2;
+        const int row = (ew & 3) * 32 + lane;
         for (int i = 0; i < myTiles; i++) {
             const int b = i & 1;
             const uint32_t k = (uint32_t)i >> 1;
@@ -414,9 +430,9 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_dense_ozaki_ws(uint4* __restr
             const IT g = ((IT)blockIdx.x + (IT)i * gridDim.x) * 128 + (IT)row;
             const bool valid = g < numGroups;
             const IT base = valid ? insert_zeros(g, p.q) : (IT)0;
-            const uint32_t lanes = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)b * kWsAccCols;
+            const uint32_t lanes = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)b * W::kAccCols;
 #pragma unroll
-            for (int ch = 0; ch < D / 4; ch++) {
+            for (int ch = cg; ch < D / 4; ch += W::EPQ) {
                 float acc[kOzAccs][8];
 #pragma unroll
                 for (int u = 0; u < kOzAccs; u++) {
@@ -464,7 +480,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_dense_ozaki_ws(uint4* __restr
             if (i >= 2 && !(ok = tc::mbar_wait(&accFree[b], (k - 1) & 1, kTcWaitLimit))) break;
             tc::fence_after_sync();
             const unsigned char* sA = smem + b * kOzSlices * S::A16;
-            const uint32_t dst = tmem + (uint32_t)b * kWsAccCols;
+            const uint32_t dst = tmem + (uint32_t)b * W::kAccCols;
 #pragma unroll
             for (int u = 0; u < kOzSlices; u++) {
                 const int acc = u < kOzAccs ? u : kOzAccs - 1;
@@ -495,7 +511,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_dense_ozaki_ws(uint4* __restr
     if (!ok) atomicExch(&g_tcTimeout, 1);
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_free<2 * kWsAccCols>(tmem);
+    if (warp == 0) tc::tmem_free<2 * W::kAccCols>(tmem);
 }
 
 // ------------------------------------------------------------- complex64
@@ -747,15 +763,19 @@ static int dense_tc_run(State* s, const unsigned* targs, const double* g) {
         if ((rc = set_smem(kern, smem))) return rc;
         kern<<<grid, kTcThreads, smem, ctx().stream>>>((float2*)s->amps, groups, p, (const uint4*)ctx().scratch);
     } else if constexpr (KT == 3) {
-        // warp-specialised: two A buffers and two accumulator sets (256 TMEM columns) per CTA;
-        // shared memory padded so that no third CTA can join an SM's 512 columns
+        // warp-specialised: two A buffers and two accumulator sets per CTA; shared memory
+        // padded so that no more than kMinBlocks CTAs share an SM's 512 TMEM columns
+        using W = WsShape<KT>;
         const size_t perSMws = ctx().smemOptin + 1024;
-        const size_t wsSmem = std::max<size_t>(2 * kOzSlices * S::A16 + kOzBCopies * kOzSlices * S::B16,
-                                               std::min<size_t>(perSMws / 3 + 1, perSMws / 2 - 3 * 1024));
-        auto kern = k_dense_ozaki_ws<IT>;
+        const size_t wsSmem = std::max<size_t>(
+            2 * kOzSlices * S::A16 + kOzBCopies * kOzSlices * S::B16,
+            std::min<size_t>(perSMws / (W::kMinBlocks + 1) + 1, perSMws / W::kMinBlocks - 3 * 1024));
+        auto kern = k_dense_ozaki_ws<IT, KT>;
         if ((rc = set_smem(kern, wsSmem))) return rc;
-        const unsigned wsGrid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(tiles, (uint64_t)ctx().numSMs * 2));
-        kern<<<wsGrid, kWsThreads, wsSmem, ctx().stream>>>((uint4*)s->amps, groups, p, (const uint4*)ctx().scratch);
+        const unsigned wsGrid = (unsigned)std::max<uint64_t>(
+            1, std::min<uint64_t>(tiles, (uint64_t)ctx().numSMs * W::kMinBlocks));
+        kern<<<wsGrid, ws_threads<KT>(), wsSmem, ctx().stream>>>((uint4*)s->amps, groups, p,
+                                                                (const uint4*)ctx().scratch);
     } else if constexpr (S::kOzakiFits) {
         auto kern = k_dense_ozaki<IT, KT>;
         if ((rc = set_smem(kern, smem))) return rc;
