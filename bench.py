@@ -59,8 +59,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the e2e, FP32 and native-FP64 legs")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the adjoint, batched and 32-qubit precision legs")
-    ap.add_argument("--legs", default="adjoint,batched,precision32",
-                    help="comma-separated forms to run (adjoint, batched, precision32)")
+    ap.add_argument("--legs", default="adjoint,batched,precision32,fusion",
+                    help="comma-separated forms to run (adjoint, batched, precision32, fusion)")
     ap.add_argument("--form-scale", default="full", choices=["full", "small"],
                     help="small: the forms at reduced sizes, for profiling captures")
     return ap.parse_args()
@@ -421,7 +421,7 @@ def gpu_arm(args, world, rank, local):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args, circuits, gates)
     if not args.no_forms:
-        legs = {"adjoint": adjoint_leg, "batched": batch_leg, "precision32": precision_leg}
+        legs = {"adjoint": adjoint_leg, "batched": batch_leg, "precision32": precision_leg, "fusion": fusion_leg}
         for name in [x for x in args.legs.split(",") if x]:
             if name not in legs:
                 result[name] = {"error": "unknown leg"}
@@ -562,6 +562,33 @@ def precision_leg(dfs, circuits, small=False):
     res["expec_abs_err"] = abs(expec["c64"] - expec["c128"])
     res["expec_rel_err"] = res["expec_abs_err"] / float(np.sum(np.abs(coeffs)))
     res["fidelity"] = fid
+    return res
+
+
+def fusion_leg(dfs, circuits, small=False):
+    """Gate fusion of forward passes through the circuit runtime, against the same circuit
+    operation by operation: the gate mix (random qubits: short runs) and a circuit of gates
+    on the 11 lowest qubits (long runs)."""
+    n = 26 if small else NUM_QUBITS
+    res = {"workload": f"sv{n}: gate mix of {NUM_GATES} gates, and {NUM_GATES} gates on the 11 lowest qubits "
+                       "(every 20th on any qubit); Circuit.apply with and without fusion"}
+    for name, gates in (("gate_mix", circuits.gate_mix(n, NUM_GATES, CIRCUIT_SEED)),
+                        ("low_qubit", circuits.low_qubit_mix(n, NUM_GATES, 11, seed=CIRCUIT_SEED))):
+        circ, params = circuits.record(dfs, n, gates)
+        for prec in ("c128", "c64"):
+            psi = dfs.StateVector(n, precision=prec)
+            psi.setRandomAmps(seed=STATE_SEED, normalise=True)
+            times = {}
+            for fusion in (False, True):
+                circ.fusion = fusion
+                circ.apply(psi, params)
+                times[fusion] = _sync_time(dfs, lambda: circ.apply(psi, params))[0]
+            runs, fused_ops = circ.fusedRuns(prec)
+            res[f"{name}_{prec}"] = {"gates_per_s_fused": len(gates) / (times[True] * 1e-3),
+                                     "gates_per_s_unfused": len(gates) / (times[False] * 1e-3),
+                                     "speedup": times[False] / times[True], "runs": runs, "fused_ops": fused_ops}
+            psi.free()
+        circ.free()
     return res
 
 

@@ -126,6 +126,8 @@ PROTOTYPES = {
     "dfs_circuit_oneQubitDepolarising": [_H, _U, _I, _D],
     "dfs_circuit_twoQubitDepolarising": [_H, _U, _U, _I, _D],
     "dfs_circuit_damping": [_H, _U, _I, _D],
+    "dfs_circuit_set_fusion": [_H, _I],
+    "dfs_circuit_fused_runs": [_H, _I, _UP, _UP],
     "dfs_circuit_apply": [_H, _H, _DP],
     "dfs_circuit_expec": [_H, _H, _DP, _DP, _U, _UP, _DP],
     "dfs_circuit_gradient": [_H, _DP, _DP],

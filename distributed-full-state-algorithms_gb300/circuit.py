@@ -138,6 +138,22 @@ class Circuit:
         call("dfs_circuit_damping", self._h, int(qb), i, v)
         return self
 
+    # ---- gate fusion of forward passes ----
+    @property
+    def fusion(self) -> bool:
+        return getattr(self, "_fusion", True)
+
+    @fusion.setter
+    def fusion(self, enable: bool) -> None:
+        call("dfs_circuit_set_fusion", self._h, 1 if enable else 0)
+        self._fusion = bool(enable)
+
+    def fusedRuns(self, precision: str = "c128"):
+        """(runs, operations in runs) of the fusion plan for a precision."""
+        r, o = C.c_uint(), C.c_uint()
+        call("dfs_circuit_fused_runs", self._h, _lib.PRECISIONS[precision], C.byref(r), C.byref(o))
+        return r.value, o.value
+
     # ---- execution ----
     def _params(self, params):
         p = np.ascontiguousarray(np.asarray(params if params is not None else [], dtype=np.float64).ravel())

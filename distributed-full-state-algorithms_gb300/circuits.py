@@ -87,6 +87,34 @@ def gate_mix(num_qubits: int, num_gates: int, seed: int, dense_k: Sequence[int] 
     return gates
 
 
+def low_qubit_mix(num_qubits: int, num_gates: int, low: int, seed: int) -> list[Gate]:
+    """Gates on the `low` lowest qubits (one-target Haar, two-control, swap, weight-3 Pauli
+    gadget, two-qubit phase gadget, Pauli tensor, two-target Haar) with every 20th on any
+    qubit: a circuit with long runs of operations inside a small qubit set, the case that
+    gate fusion targets."""
+    rng = np.random.default_rng(seed)
+    gates = []
+    for i in range(num_gates):
+        span = num_qubits if i % 20 == 19 else low
+        q = [int(x) for x in rng.choice(span, size=3, replace=False)]
+        kind = i % 7
+        if kind == 0:
+            gates.append(Gate("one_targ", (q[0],), matrix=haar_unitary(rng, 2)))
+        elif kind == 1:
+            gates.append(Gate("ctrl", (q[0],), controls=(q[1], q[2]), matrix=haar_unitary(rng, 2)))
+        elif kind == 2:
+            gates.append(Gate("swap", (q[0], q[1])))
+        elif kind == 3:
+            gates.append(Gate("pauli_gadget", tuple(q), paulis=(1, 2, 3), param=float(rng.normal())))
+        elif kind == 4:
+            gates.append(Gate("phase_gadget", (q[0], q[1]), param=float(rng.normal())))
+        elif kind == 5:
+            gates.append(Gate("pauli_tensor", (q[0], q[2]), paulis=(2, 1)))
+        else:
+            gates.append(Gate("many_targ", (q[0], q[1]), matrix=haar_unitary(rng, 4)))
+    return gates
+
+
 def dm_layers(num_qubits: int, num_layers: int, seed: int, max_prob: float = 0.1) -> list[Gate]:
     """Layers of a 2-target Haar unitary on a random pair followed by one/two-qubit
     dephasing, depolarising and damping with prob ~ U[0, max_prob]."""

@@ -102,11 +102,11 @@ static void release(Batch* b) {
     if (b->stream) cudaStreamDestroy(b->stream);
 }
 
-static void pauli_op_masks(const CircOp& op, batch::OpD& d, int* numY) {
+static void pauli_op_masks(const CircOp& op, const unsigned* qmap, batch::OpD& d, int* numY) {
     uint32_t mX = 0, mYZ = 0;
     int y = 0, top = -1;
     for (size_t i = 0; i < op.targs.size(); i++) {
-        unsigned p = op.kind == OP_PHASE_GADGET ? 3u : op.paulis[i], q = op.targs[i];
+        unsigned p = op.kind == OP_PHASE_GADGET ? 3u : op.paulis[i], q = qmap ? qmap[op.targs[i]] : op.targs[i];
         if (p == 1 || p == 2) {
             mX |= 1u << q;
             top = std::max(top, (int)q);
@@ -126,81 +126,89 @@ static void sorted_positions(std::vector<unsigned> qs, batch::OpD& d) {
     for (size_t i = 0; i < qs.size(); i++) d.q[i] = (uint8_t)qs[i];
 }
 
-// device form of one recorded operation; returns an error for what the batch cannot run
-static int lower_op(Batch* b, unsigned ci, const CircOp& op, batch::OpD& d) {
+int lower_circ_op(const CircOp& op, const unsigned* qmap, batch::OpD& d, std::vector<double>& mats, int* numY,
+                  const char* who) {
     memset(&d, 0, sizeof d);
     d.gradRow = -1;
-    int paramIdx = -1;
-    double theta = 0;
-    auto add_mats = [&](size_t dim) {
-        d.mat = (uint32_t)b->mats.size();
-        b->mats.insert(b->mats.end(), op.gate.begin(), op.gate.end());
-        b->mats.insert(b->mats.end(), op.gateAdj.begin(), op.gateAdj.end());
-        (void)dim;
+    *numY = 0;
+    auto Q = [&](unsigned q) { return qmap ? qmap[q] : q; };
+    auto add_mats = [&]() {
+        d.mat = (uint32_t)mats.size();
+        mats.insert(mats.end(), op.gate.begin(), op.gate.end());
+        mats.insert(mats.end(), op.gateAdj.begin(), op.gateAdj.end());
     };
     switch (op.kind) {
         case OP_ONE_TARG:
         case OP_CTRL: {
             if (op.ctrls.size() > (size_t)batch::kMaxCtrls)
-                return fail(DFS_ERR_TOO_LARGE, "batched gates take at most %d controls", batch::kMaxCtrls);
-            std::vector<unsigned> qs(op.ctrls);
-            qs.push_back(op.targs[0]);
+                return fail(DFS_ERR_TOO_LARGE, "%s gates take at most %d controls", who, batch::kMaxCtrls);
+            std::vector<unsigned> qs;
+            for (unsigned c : op.ctrls) qs.push_back(Q(c));
+            qs.push_back(Q(op.targs[0]));
             sorted_positions(qs, d);
             uint32_t m = 0;
             for (unsigned q : qs) m |= 1u << q;
             d.kind = batch::BK_PAIR;
             d.setMask = m;
-            d.tbit = 1u << op.targs[0];
-            add_mats(2);
+            d.tbit = 1u << Q(op.targs[0]);
+            add_mats();
             break;
         }
         case OP_SWAP: {
             d.kind = batch::BK_SWAP;
-            sorted_positions(op.targs, d);
-            d.setMask = 1u << std::min(op.targs[0], op.targs[1]);
-            d.tbit = 1u << std::max(op.targs[0], op.targs[1]);
+            const unsigned a = Q(op.targs[0]), b = Q(op.targs[1]);
+            sorted_positions({a, b}, d);
+            d.setMask = 1u << std::min(a, b);
+            d.tbit = 1u << std::max(a, b);
             break;
         }
         case OP_MANY_TARG: {
-            if (op.targs.size() > 3) return fail(DFS_ERR_TOO_LARGE, "batched dense gates take at most 3 targets");
+            if (op.targs.size() > 3) return fail(DFS_ERR_TOO_LARGE, "%s dense gates take at most 3 targets", who);
             d.kind = batch::BK_DENSE;
             d.k = (uint8_t)op.targs.size();
-            sorted_positions(op.targs, d);
+            std::vector<unsigned> qs;
+            for (unsigned t : op.targs) qs.push_back(Q(t));
+            sorted_positions(qs, d);
             for (unsigned c = 0; c < (1u << d.k); c++) {
                 uint32_t o = 0;
-                for (unsigned i = 0; i < d.k; i++) o |= ((c >> i) & 1u) << op.targs[i];
+                for (unsigned i = 0; i < d.k; i++) o |= ((c >> i) & 1u) << qs[i];
                 d.off[c] = o;
             }
-            add_mats((size_t)1 << d.k);
+            add_mats();
             break;
         }
         case OP_PAULI_TENSOR: {
-            int y;
-            pauli_op_masks(op, d, &y);
+            pauli_op_masks(op, qmap, d, numY);
             d.kind = batch::BK_TENSOR;
-            d.powY = (uint8_t)(y & 3);
+            d.powY = (uint8_t)(*numY & 3);
             break;
         }
         case OP_PAULI_GADGET:
         case OP_PHASE_GADGET: {
-            int y;
-            pauli_op_masks(op, d, &y);
+            pauli_op_masks(op, qmap, d, numY);
             d.kind = d.maskX ? batch::BK_GADGET : batch::BK_DIAG;
-            d.powY = (uint8_t)((y + 1) & 3);
-            paramIdx = op.param;
-            theta = op.value;
-            if (op.param >= 0) {
-                d.gradRow = (int32_t)b->rows.size();
-                b->rows.push_back({ci, op.param, y});
-            }
+            d.powY = (uint8_t)((*numY + 1) & 3);
             break;
         }
-        default: return fail(DFS_ERR_STATE_KIND, "channels cannot be batched (statevector circuits only)");
+        default: return fail(DFS_ERR_STATE_KIND, "%s circuits hold no channels (statevector circuits only)", who);
     }
-    if (!op.invertible) return fail(DFS_ERR_INVALID_ARG, "batched circuits take unitary gates only");
+    if (!op.invertible) return fail(DFS_ERR_INVALID_ARG, "%s circuits take unitary gates only", who);
+    return DFS_SUCCESS;
+}
+
+// device form of one recorded operation; returns an error for what the batch cannot run
+static int lower_op(Batch* b, unsigned ci, const CircOp& op, batch::OpD& d) {
+    int y = 0;
+    int rc = lower_circ_op(op, nullptr, d, b->mats, &y, "batched");
+    if (rc) return rc;
+    const bool gadget = op.kind == OP_PAULI_GADGET || op.kind == OP_PHASE_GADGET;
+    if (gadget && op.param >= 0) {
+        d.gradRow = (int32_t)b->rows.size();
+        b->rows.push_back({ci, op.param, y});
+    }
     d.trig = (uint32_t)b->opParam.size();
-    b->opParam.push_back(paramIdx >= 0 ? (int)(b->paramOff[ci] + paramIdx) : -1);
-    b->opTheta.push_back(theta);
+    b->opParam.push_back(gadget && op.param >= 0 ? (int)(b->paramOff[ci] + op.param) : -1);
+    b->opTheta.push_back(gadget ? op.value : 0.0);
     return DFS_SUCCESS;
 }
 

@@ -34,6 +34,8 @@ struct CircOp {
     bool is_channel() const { return kind >= OP_DEPH1; }
 };
 
+struct FusedPlan;  // circuit.cu
+
 struct Circuit {
     unsigned numQubits = 0;
     int isDM = 0;
@@ -45,6 +47,10 @@ struct Circuit {
     std::vector<State*> ckpt;  // one per non-invertible operation, in order
     void* dev = nullptr;       // terms | partial rows | row sums
     size_t devBytes = 0;
+    // gate fusion of forward passes (statevector circuits of unitary operations): the run
+    // plan, built on first use for the state's precision and dropped when operations change
+    bool fusion = true;
+    FusedPlan* plan = nullptr;
     // the latest forward pass
     bool haveForward = false;
     std::vector<double> fwdParams;
@@ -52,6 +58,16 @@ struct Circuit {
     std::vector<double> coeffs;
     std::vector<unsigned> paulis;
 };
+
+namespace batch {
+struct OpD;
+}
+// the device record of a unitary statevector operation with its qubits mapped through
+// qmap (nullptr: unchanged); gates append themselves and their adjoints to mats.  Fails
+// for what the device records cannot hold (channels, non-unitary or > 3-target dense
+// gates, > 6 controls); `who` names the caller in the message.
+int lower_circ_op(const CircOp& op, const unsigned* qmap, batch::OpD& d, std::vector<double>& mats, int* numY,
+                  const char* who);
 
 }  // namespace dfs
 

@@ -1,0 +1,26 @@
+// fused.hpp -- one pass of a fused run of circuit operations (k_fused.cu); the circuit
+// runtime (circuit.cu) plans the runs.
+#pragma once
+
+#include "batch.hpp"
+
+namespace dfs {
+
+constexpr int kFuseMaxTileQubits = 13;
+
+struct FusedLaunch {
+    QList tileQ;        // the tile qubits, sorted: zero bits of a tile's base index
+    uint8_t q[16];      // the same positions, ascending (local bit b <-> qubit q[b])
+    uint32_t m;         // tile qubits
+    uint64_t numTiles;  // 2^(n - m)
+    const batch::OpD* ops;  // the run's operations with tile-local qubit positions
+    uint32_t numOps;
+    const double* mats;
+    const double2* trig;
+};
+
+// tile qubits per precision (64 KiB of shared memory per tile)
+int fuse_tile_qubits(int precision);
+int fused_run(State* s, const FusedLaunch& a);
+
+}  // namespace dfs

@@ -1,0 +1,61 @@
+"""Gate fusion of forward passes: runs of operations applied in one pass over the state
+with the tile held in shared memory equal the operation-by-operation pass (and the oracle)."""
+import numpy as np
+import pytest
+
+from adjoint_ref import circuits
+from helpers import TOL, gaussian_state, haar, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _low_qubit_circuit(rng, n, num, low):
+    return circuits.low_qubit_mix(n, num, low, seed=int(rng.integers(1 << 30)))
+
+
+@pytest.mark.parametrize("prec", ["c128", "c128_native", "c64"])
+def test_fused_forward_equals_unfused_and_oracle(dfs, oracle, prec, rng):
+    n = 20
+    for gates in (_low_qubit_circuit(rng, n, 80, 11), circuits.gate_mix(n, 60, seed=int(rng.integers(1 << 30)))):
+        circ, params = circuits.record(dfs, n, gates)
+        runs, fused_ops = circ.fusedRuns(prec)
+        a0 = gaussian_state(rng, 1 << n, normalise=True)
+        psi = dfs.StateVector(n, precision=prec)
+        psi.setAmps(a0)
+        start = psi.getAllVecAmps()
+        circ.fusion = True
+        circ.apply(psi, params)
+        fused = psi.getAllVecAmps()
+        psi.setAmps(a0)
+        circ.fusion = False
+        circ.apply(psi, params)
+        plain = psi.getAllVecAmps()
+        # complex128 amplitudes stay double-float (48 bits) between the operations of a run
+        assert rel_err(fused, plain) <= (TOL[prec] if prec != "c64" else 1e-6)
+        if prec != "c64":
+            ref = start.copy()
+            circuits.apply_to(oracle, ref, gates)
+            assert rel_err(fused, ref) <= TOL[prec]
+    # the low-qubit circuit fuses most of its operations (native FP64 never fuses)
+    circ, params = circuits.record(dfs, n, _low_qubit_circuit(rng, n, 80, 11))
+    runs, fused_ops = circ.fusedRuns(prec)
+    if prec == "c128_native":
+        assert runs == 0
+    else:
+        assert runs >= 1 and fused_ops >= 40, (runs, fused_ops)
+
+
+def test_fused_forward_in_gradients(dfs, rng):
+    n = 19
+    gates = _low_qubit_circuit(rng, n, 60, 10)
+    coeffs, paulis = circuits.pauli_sum(n, 12, seed=4)
+    circ, params = circuits.record(dfs, n, gates)
+    init = dfs.StateVector(n)
+    init.setRandomAmps(seed=3, normalise=True)
+    out = {}
+    for fusion in (True, False):
+        circ.fusion = fusion
+        loss = circ.expectation(init, params, coeffs, paulis)
+        out[fusion] = (loss, circ.gradient(params))
+    assert abs(out[True][0] - out[False][0]) <= 1e-12 * np.sum(np.abs(coeffs))
+    assert np.max(np.abs(out[True][1] - out[False][1])) <= 1e-10 * max(1.0, np.max(np.abs(out[False][1])))
