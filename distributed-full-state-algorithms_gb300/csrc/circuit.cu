@@ -329,9 +329,9 @@ static std::vector<AdjTerm> make_terms(unsigned n, const double* coeffs, unsigne
 // 1.07x for the random gate mix's runs of ~5); in complex128 the double-float arithmetic
 // of an operation in shared memory (~3.8 ms) nearly equals a separate HBM-bound kernel
 // (5.5 ms), so only long runs pay (1.25x at 12.5 operations, 0.7x at ~4).
-static size_t min_run(int precision) {
+static size_t min_run(int precision, bool backward) {
     switch (precision) {
-        case DFS_C64: return 3;
+        case DFS_C64: return backward ? 2 : 3;  // a backward step moves twice the bytes
         case DFS_C128: return 8;
         default: return SIZE_MAX;  // native FP64 arithmetic is bound by the FP64 pipe either way
     }
@@ -356,14 +356,19 @@ struct FusedPlan {
     std::vector<double2> hTrig;
 };
 
-static void fused_free(Circuit* c) {
-    if (!c->plan) return;
-    if (c->plan->dev) {
+static void plan_free(FusedPlan*& pl) {
+    if (!pl) return;
+    if (pl->dev) {
         cudaStreamSynchronize(ctx().stream);
-        cudaFree(c->plan->dev);
+        cudaFree(pl->dev);
     }
-    delete c->plan;
-    c->plan = nullptr;
+    delete pl;
+    pl = nullptr;
+}
+
+static void fused_free(Circuit* c) {
+    plan_free(c->plan);
+    plan_free(c->planB);
 }
 
 static std::vector<unsigned> op_qubits(const CircOp& op) {
@@ -387,12 +392,16 @@ static bool fusable(const CircOp& op, int precision) {
     }
 }
 
-// builds the plan for this precision, or leaves c->plan null when fusion does not apply
-static int fused_plan(Circuit* c, int precision) {
-    if (c->plan && c->plan->precision == precision) return DFS_SUCCESS;
-    fused_free(c);
+static bool param_gadget(const CircOp& op) {
+    return (op.kind == OP_PAULI_GADGET || op.kind == OP_PHASE_GADGET) && op.param >= 0;
+}
+
+// the runs of a plan with m tile qubits; for the backward sweep (two tiles per CTA, so
+// m is one less) each run's parametrised gadgets get gradRow = their order in the sweep
+// (last operation first), and a run holds at most kFuseMaxParams of them
+static int build_plan(const Circuit* c, int precision, unsigned m, bool backward, FusedPlan** out) {
+    *out = nullptr;
     const unsigned n = c->numQubits;
-    const unsigned m = (unsigned)fuse_tile_qubits(precision);
     if (c->isDM || n < m + 6) return DFS_SUCCESS;  // at least 64 tiles
     for (const CircOp& op : c->ops)
         if (!op.invertible) return DFS_SUCCESS;
@@ -405,14 +414,17 @@ static int fused_plan(Circuit* c, int precision) {
     while (i < numOps) {
         uint64_t Q = 0xFull;  // the four lowest qubits
         size_t j = i;
+        int params = 0;
         while (j < numOps && fusable(c->ops[j], precision)) {
             uint64_t q2 = Q;
             for (unsigned q : op_qubits(c->ops[j])) q2 |= 1ull << q;
             if ((unsigned)__builtin_popcountll(q2) > m) break;
+            if (backward && param_gadget(c->ops[j]) && params == kFuseMaxParams) break;
+            params += param_gadget(c->ops[j]);
             Q = q2;
             j++;
         }
-        if (j - i < std::max<size_t>(2, min_run(precision))) {
+        if (j - i < std::max<size_t>(2, min_run(precision, backward))) {
             const size_t end = std::max(j, i + 1);
             for (size_t o = i; o < end; o++) pl->segs.push_back({o, o + 1, false, 0, {}, 0});
             i = end;
@@ -428,6 +440,7 @@ static int fused_plan(Circuit* c, int precision) {
                 seg.q[pos] = (uint8_t)q;
                 qmap[q] = pos++;
             }
+        int order = params;  // the sweep meets the run's last gadget first
         for (size_t o = i; o < j; o++) {
             batch::OpD d;
             int y = 0;
@@ -437,6 +450,7 @@ static int fused_plan(Circuit* c, int precision) {
                 return rc;
             }
             d.trig = (uint32_t)ops.size();
+            d.gradRow = backward && param_gadget(c->ops[o]) ? --order : -1;
             ops.push_back(d);
             pl->devOpOf.push_back(o);
         }
@@ -465,8 +479,51 @@ static int fused_plan(Circuit* c, int precision) {
         }
         pl->hTrig.resize(ops.size());
     }
-    c->plan = pl;
+    *out = pl;
     return DFS_SUCCESS;
+}
+
+// the forward plan for this precision, or c->plan null when fusion does not apply
+static int fused_plan(Circuit* c, int precision) {
+    if (c->plan && c->plan->precision == precision) return DFS_SUCCESS;
+    plan_free(c->plan);
+    return build_plan(c, precision, (unsigned)fuse_tile_qubits(precision), false, &c->plan);
+}
+
+static int fused_plan_backward(Circuit* c, int precision) {
+    if (c->planB && c->planB->precision == precision) return DFS_SUCCESS;
+    plan_free(c->planB);
+    return build_plan(c, precision, (unsigned)fuse_tile_qubits(precision) - 1, true, &c->planB);
+}
+
+// (cos, sin) of every fused gadget's angle, staged to the plan's device table
+static int upload_angles(const Circuit* c, FusedPlan* pl, const double* params) {
+    if (pl->hTrig.empty()) return DFS_SUCCESS;
+    for (size_t d = 0; d < pl->devOpOf.size(); d++) {
+        const CircOp& op = c->ops[pl->devOpOf[d]];
+        const bool gadget = op.kind == OP_PAULI_GADGET || op.kind == OP_PHASE_GADGET;
+        const double th = gadget ? op.val(params) : 0.0;
+        pl->hTrig[d] = make_double2(std::cos(th), std::sin(th));
+    }
+    // from pageable memory: the call returns once the table is staged, so the host vector
+    // may change at the next pass while the kernels reading it are still queued
+    cudaError_t e = cudaMemcpyAsync(pl->dTrig, pl->hTrig.data(), pl->hTrig.size() * sizeof(double2),
+                                    cudaMemcpyHostToDevice, ctx().stream);
+    return e == cudaSuccess ? DFS_SUCCESS : cuda_fail(e, "fusion angles");
+}
+
+static FusedLaunch launch_of(const FusedPlan* pl, const FusedSeg& seg, unsigned n) {
+    FusedLaunch L{};
+    std::vector<unsigned> tq(seg.q, seg.q + seg.m);
+    L.tileQ = make_qlist(tq);
+    for (unsigned b = 0; b < seg.m; b++) L.q[b] = seg.q[b];
+    L.m = seg.m;
+    L.numTiles = (1ull << n) >> seg.m;
+    L.ops = pl->dOps + seg.opBegin;
+    L.numOps = (uint32_t)(seg.last - seg.first);
+    L.mats = pl->dMats;
+    L.trig = pl->dTrig;
+    return L;
 }
 
 // ---------------------------------------------------------------- passes
@@ -478,37 +535,14 @@ static int forward(Circuit* c, State* s, const double* params, bool keepCheckpoi
     }
     if (c->fusion && c->plan && c->plan->precision == s->precision) {
         FusedPlan* pl = c->plan;
-        if (!pl->hTrig.empty()) {
-            for (size_t d = 0; d < pl->devOpOf.size(); d++) {
-                const CircOp& op = c->ops[pl->devOpOf[d]];
-                const bool gadget = op.kind == OP_PAULI_GADGET || op.kind == OP_PHASE_GADGET;
-                const double th = gadget ? op.val(params) : 0.0;
-                pl->hTrig[d] = make_double2(std::cos(th), std::sin(th));
-            }
-            // from pageable memory: the call returns once the table is staged, so the host
-            // vector may change at the next pass while these kernels are still queued
-            cudaError_t e = cudaMemcpyAsync(pl->dTrig, pl->hTrig.data(), pl->hTrig.size() * sizeof(double2),
-                                            cudaMemcpyHostToDevice, ctx().stream);
-            if (e != cudaSuccess) return cuda_fail(e, "fusion angles");
-        }
-        const uint64_t numAmps = 1ull << s->numQubits;
+        int rc = upload_angles(c, pl, params);
+        if (rc) return rc;
         for (const FusedSeg& seg : pl->segs) {
-            int rc;
             if (!seg.fused) {
                 const CircOp& op = c->ops[seg.first];
                 rc = apply_op(s, op, op.val(params), false);
             } else {
-                FusedLaunch L{};
-                std::vector<unsigned> tq(seg.q, seg.q + seg.m);
-                L.tileQ = make_qlist(tq);
-                for (unsigned b = 0; b < seg.m; b++) L.q[b] = seg.q[b];
-                L.m = seg.m;
-                L.numTiles = numAmps >> seg.m;
-                L.ops = pl->dOps + seg.opBegin;
-                L.numOps = (uint32_t)(seg.last - seg.first);
-                L.mats = pl->dMats;
-                L.trig = pl->dTrig;
-                rc = fused_run(s, L);
+                rc = fused_run(s, launch_of(pl, seg, s->numQubits));
             }
             if (rc) return rc;
         }
@@ -558,7 +592,8 @@ static int backward(Circuit* c, const double* params, double* grad) {
     }
     std::vector<RowUse> uses;
     size_t k = c->ckpt.size();
-    for (size_t i = c->ops.size(); i-- > 0;) {
+    auto undo = [&](size_t i) -> int {
+        int rc = DFS_SUCCESS;
         const CircOp& op = c->ops[i];
         const double v = op.val(params);
         const bool gadget = op.kind == OP_PAULI_GADGET || op.kind == OP_PHASE_GADGET;
@@ -578,7 +613,7 @@ static int backward(Circuit* c, const double* params, double* grad) {
             double2* row = L.parts + (size_t)uses.size() * L.cols;
             if ((rc = adj_gadget_step(st, ad, mX, mYZ, numY, v, row))) return rc;
             uses.push_back({op.param, 0, numY, c->isDM ? 1.0 : 2.0});
-            continue;
+            return DFS_SUCCESS;
         }
         if (op.is_channel()) {
             State* before = c->ckpt[--k];
@@ -597,8 +632,7 @@ static int backward(Circuit* c, const double* params, double* grad) {
                 channel_mats1(op, n, v, &m);
                 rc = adj_channel_step(ad, st, &m, nullptr, row);
             }
-            if (rc) return rc;
-            continue;
+            return rc;
         }
         // unitary (or recorded non-unitary) operations without parameters
         if ((rc = apply_op(ad, op, v, true))) return rc;
@@ -608,6 +642,38 @@ static int backward(Circuit* c, const double* params, double* grad) {
             State* before = c->ckpt[--k];
             if ((rc = dfs_state_copy(static_cast<dfs_state>(st), static_cast<dfs_state>(before)))) return rc;
         }
+        return DFS_SUCCESS;
+    };
+    // statevector circuits: runs of operations undone in one pass over both vectors
+    FusedPlan* pl = nullptr;
+    if (c->fusion && !c->isDM) {
+        if ((rc = fused_plan_backward(c, st->precision))) return rc;
+        pl = c->planB;
+    }
+    if (pl) {
+        if ((rc = upload_angles(c, pl, params))) return rc;
+        for (size_t g = pl->segs.size(); g-- > 0;) {
+            const FusedSeg& seg = pl->segs[g];
+            if (!seg.fused) {
+                if ((rc = undo(seg.first))) return rc;
+                continue;
+            }
+            const unsigned rowBase = (unsigned)uses.size();
+            if ((rc = fused_run_backward(st, ad, launch_of(pl, seg, n), L.parts, L.cols, rowBase))) return rc;
+            for (size_t o = seg.last; o-- > seg.first;) {
+                const CircOp& op = c->ops[o];
+                if (!param_gadget(op)) continue;
+                std::vector<unsigned> ps =
+                    op.kind == OP_PAULI_GADGET ? op.paulis : std::vector<unsigned>(op.targs.size(), 3);
+                uint64_t mX, mYZ;
+                int numY;
+                pauli_masks(op.targs, ps, 0, &mX, &mYZ, &numY);
+                uses.push_back({op.param, 0, numY, 2.0});
+            }
+        }
+    } else {
+        for (size_t i = c->ops.size(); i-- > 0;)
+            if ((rc = undo(i))) return rc;
     }
     std::vector<double2> sums(uses.size());
     if (!uses.empty()) {

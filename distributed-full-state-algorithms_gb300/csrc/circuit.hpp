@@ -50,7 +50,8 @@ struct Circuit {
     // gate fusion of forward passes (statevector circuits of unitary operations): the run
     // plan, built on first use for the state's precision and dropped when operations change
     bool fusion = true;
-    FusedPlan* plan = nullptr;
+    FusedPlan* plan = nullptr;   // forward runs
+    FusedPlan* planB = nullptr;  // backward runs (two tiles, state and adjoint, per CTA)
     // the latest forward pass
     bool haveForward = false;
     std::vector<double> fwdParams;

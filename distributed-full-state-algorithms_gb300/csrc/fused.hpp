@@ -7,6 +7,7 @@
 namespace dfs {
 
 constexpr int kFuseMaxTileQubits = 13;
+constexpr int kFuseMaxParams = 64;  // parametrised operations in one backward run
 
 struct FusedLaunch {
     QList tileQ;        // the tile qubits, sorted: zero bits of a tile's base index
@@ -22,5 +23,10 @@ struct FusedLaunch {
 // tile qubits per precision (64 KiB of shared memory per tile)
 int fuse_tile_qubits(int precision);
 int fused_run(State* s, const FusedLaunch& a);
+// the backward sweep of a run (operations undone last to first on the state st and the
+// adjoint ad); the run's parametrised gadgets carry gradRow = their order in the sweep,
+// and this CTA's partial sum of gadget p lands in partials[(rowBase + p) * cols + CTA]
+int fused_run_backward(State* st, State* ad, const FusedLaunch& a, double2* partials, unsigned cols,
+                       unsigned rowBase);
 
 }  // namespace dfs
