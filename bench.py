@@ -59,8 +59,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the e2e, FP32 and native-FP64 legs")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the adjoint, batched and 32-qubit precision legs")
-    ap.add_argument("--legs", default="adjoint,batched,precision32,fusion",
-                    help="comma-separated forms to run (adjoint, batched, precision32, fusion)")
+    ap.add_argument("--legs", default="adjoint,batched,precision32,fusion,dm12",
+                    help="comma-separated forms to run (adjoint, batched, precision32, fusion, dm12)")
     ap.add_argument("--form-scale", default="full", choices=["full", "small"],
                     help="small: the forms at reduced sizes, for profiling captures")
     return ap.parse_args()
@@ -421,7 +421,8 @@ def gpu_arm(args, world, rank, local):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args, circuits, gates)
     if not args.no_forms:
-        legs = {"adjoint": adjoint_leg, "batched": batch_leg, "precision32": precision_leg, "fusion": fusion_leg}
+        legs = {"adjoint": adjoint_leg, "batched": batch_leg, "precision32": precision_leg, "fusion": fusion_leg,
+                "dm12": dm_leg}
         for name in [x for x in args.legs.split(",") if x]:
             if name not in legs:
                 result[name] = {"error": "unknown leg"}
@@ -589,6 +590,91 @@ def fusion_leg(dfs, circuits, small=False):
                                      "speedup": times[False] / times[True], "runs": runs, "fused_ops": fused_ops}
             psi.free()
         circ.free()
+    return res
+
+
+def run_reference_dm_op(ref, h, g):
+    import ctypes as C
+    L = ref.lib
+    if g.kind == "dm_many_targ":
+        t = (C.c_uint * len(g.qubits))(*g.qubits)
+        m = np.ascontiguousarray(g.matrix, dtype=np.complex128)
+        L.ref_dm_many_targ(h, t, len(g.qubits), m.ctypes.data_as(C.c_void_p))
+    elif g.kind == "deph1":
+        L.ref_dm_deph1(h, g.qubits[0], g.param)
+    elif g.kind == "deph2":
+        L.ref_dm_deph2(h, g.qubits[0], g.qubits[1], g.param)
+    elif g.kind == "depol1":
+        L.ref_dm_depol1(h, g.qubits[0], g.param)
+    elif g.kind == "depol2":
+        L.ref_dm_depol2(h, g.qubits[0], g.qubits[1], g.param)
+    elif g.kind == "damping":
+        L.ref_dm_damping(h, g.qubits[0], g.param)
+    else:
+        raise ValueError(g.kind)
+
+
+def dm_leg(dfs, circuits, small=False):
+    """The plain FP64 density-matrix workflow at 12 qubits: rho = G G^dagger / tr, 10 layers
+    of a 2-target Haar unitary and the five channels, expecPauliString over 64 strings and
+    partialTrace over 4 qubits, on the GPU; the reference's CPU code on one layer and one
+    string of the same workflow (extrapolated to the whole)."""
+    import ctypes as C
+    n = 12
+    rng = np.random.default_rng(12)
+    d = 1 << n
+    g = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    rho0 = g @ g.conj().T
+    rho0 = (rho0 / np.trace(rho0).real).reshape(-1, order="F").copy()
+    del g
+    ops = circuits.dm_layers(n, 10, seed=2024, max_prob=0.1)
+    coeffs, paulis = circuits.pauli_sum(n, 64, seed=99)
+    targets = [int(q) for q in rng.choice(n, 4, replace=False)]
+    rho = dfs.DensityMatrix(n)
+    rho.setAmps(rho0)
+    start = dfs.DensityMatrix(n)
+    start.copyFrom(rho)
+    res = {"workload": "12-qubit density matrix (2^24 amplitudes, c128): 10 layers x (2-target Haar + 5 channels), "
+                       "expecPauliString over 64 strings, partialTrace over 4 qubits"}
+    for rep in range(2):  # the first repetition warms up
+        rho.copyFrom(start)
+        t_layers = _sync_time(dfs, lambda: circuits.apply(dfs, rho, ops))[0]
+        t_expec = _sync_time(dfs, lambda: dfs.distributed_densitymatrix_expecPauliString(rho, coeffs, paulis))[0]
+        t_pt = _sync_time(dfs, lambda: dfs.distributed_densitymatrix_partialTrace(rho, targets).free())[0]
+    res["gpu_ms"] = {"layers": t_layers, "expecPauliString_64": t_expec, "partialTrace": t_pt,
+                     "total": t_layers + t_expec + t_pt}
+    rho.free()
+    start.free()
+    try:
+        from oracle.oracle import Reference
+        ref = Reference()
+        h = ref.new_state(rho0, True)
+        layer = ops[:6]
+        t0 = time.perf_counter()
+        for gate in layer:
+            run_reference_dm_op(ref, h, gate)
+        t_layer = time.perf_counter() - t0
+        c1 = np.ascontiguousarray(coeffs[:1])
+        p1 = np.ascontiguousarray(paulis[:1].ravel().astype(np.uint32))
+        out = np.zeros(2)
+        t0 = time.perf_counter()
+        ref.lib.ref_dm_expec_pauli_string(h, c1.ctypes.data_as(C.c_void_p), 1, p1.ctypes.data_as(C.c_void_p),
+                                          out.ctypes.data_as(C.c_void_p))
+        t_term = time.perf_counter() - t0
+        tq = (C.c_uint * 4)(*targets)
+        red = np.zeros(1 << (2 * (n - 4)), dtype=np.complex128)
+        t0 = time.perf_counter()
+        ref.lib.ref_dm_partial_trace(h, tq, 4, red.ctypes.data_as(C.c_void_p))
+        t_ref_pt = time.perf_counter() - t0
+        ref.free_state(h, True)
+        total = 10 * t_layer + 64 * t_term + t_ref_pt
+        res["reference_cpu"] = {"cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
+                                "kind": "reference", "layer_s": t_layer, "expec_term_s": t_term,
+                                "partialTrace_s": t_ref_pt, "total_s_extrapolated": total,
+                                "sample": "one layer and one Pauli string timed; total = 10 layers + 64 strings"}
+        res["speedup_vs_reference"] = total / (res["gpu_ms"]["total"] * 1e-3)
+    except Exception as e:  # the reference build is optional here
+        res["reference_cpu"] = {"error": f"{type(e).__name__}: {e}"}
     return res
 
 
