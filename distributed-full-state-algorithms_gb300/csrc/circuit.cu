@@ -411,8 +411,12 @@ static int build_plan(const Circuit* c, int precision, unsigned m, bool backward
     std::vector<double> mats;
     const size_t numOps = c->ops.size();
     size_t i = 0;
+    // the lowest qubits in every tile so that its loads come in runs of consecutive
+    // amplitudes (16 forward; 8 backward, whose tile is one qubit smaller, so that its runs
+    // have as many free qubits as the forward ones)
+    const uint64_t lowQubits = backward ? 0x7ull : 0xFull;
     while (i < numOps) {
-        uint64_t Q = 0xFull;  // the four lowest qubits
+        uint64_t Q = lowQubits;
         size_t j = i;
         int params = 0;
         while (j < numOps && fusable(c->ops[j], precision)) {
