@@ -523,11 +523,12 @@ DEV uint32_t to_tf32(float x) {
 }
 
 template <class IT, int KT>
-__global__ void __launch_bounds__(kTcThreads) k_dense_3xtf32(float2* __restrict__ amps, IT numGroups,
-                                                             DenseParams<IT, KT> p, const uint4* __restrict__ bsl) {
+__global__ void __launch_bounds__(2 * kTcThreads) k_dense_3xtf32(float2* __restrict__ amps, IT numGroups,
+                                                                 DenseParams<IT, KT> p, const uint4* __restrict__ bsl) {
     using S = Dense<KT>;
     constexpr int D = S::D, R = S::R;
     constexpr int KCH = S::KCH32, RC = R / KCH, DC = D / KCH;  // K chunks, reals / amplitudes per chunk
+    constexpr int DH = DC / 2, HC = R / 2;                      // per thread: amplitudes of a chunk, output reals
     constexpr uint32_t KGA = RC / 4;                            // A core matrices along K
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* sAbig = smem;
@@ -535,9 +536,11 @@ __global__ void __launch_bounds__(kTcThreads) k_dense_3xtf32(float2* __restrict_
     unsigned char* sB = smem + 2 * S::A32;  // big then small, the whole of K
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmemSlot;
-    const int tid = threadIdx.x, warp = tid >> 5;
+    // two threads per group: `half` 0 and 1 take halves of its amplitudes (and of its
+    // outputs, through the same TMEM lane quadrant from warps w and w + 4)
+    const int tid = threadIdx.x, warp = tid >> 5, row = tid & 127, half = tid >> 7;
 
-    for (int i = tid; i < (int)(2 * S::B32 / 16); i += kTcThreads) reinterpret_cast<uint4*>(sB)[i] = bsl[i];
+    for (int i = tid; i < (int)(2 * S::B32 / 16); i += 2 * kTcThreads) reinterpret_cast<uint4*>(sB)[i] = bsl[i];
     if (warp == 0) tc::tmem_alloc<S::COLS32>(&tmemSlot);
     if (tid == 0) tc::mbar_init(&mbar, 1);
     tc::fence_before_sync();
@@ -550,16 +553,16 @@ __global__ void __launch_bounds__(kTcThreads) k_dense_3xtf32(float2* __restrict_
     const IT numTiles = (numGroups + 127) / 128;
 
     for (IT tile = blockIdx.x; tile < numTiles && !timedOut; tile += gridDim.x) {
-        const IT g = tile * 128 + (IT)tid;
+        const IT g = tile * 128 + (IT)row;
         const bool valid = g < numGroups;
         const IT base = valid ? insert_zeros(g, p.q) : (IT)0;
-        float2 xv[DC];  // this chunk's amplitudes; reals ordered [re x0, im x0, re x1, ...]
+        float2 xv[DH];  // this thread's amplitudes of the chunk; reals [re x0, im x0, re x1, ...]
 #pragma unroll
-        for (int c = 0; c < DC; c++) xv[c] = valid ? amps[base + p.off[c]] : make_float2(0.f, 0.f);
+        for (int c = 0; c < DH; c++) xv[c] = valid ? amps[base + p.off[half * DH + c]] : make_float2(0.f, 0.f);
 #pragma unroll 1
         for (int ch = 0; ch < KCH; ch++) {
 #pragma unroll
-            for (int kg = 0; kg < RC / 4; kg++) {
+            for (int kg = 0; kg < RC / 8; kg++) {
                 uint32_t big[4], small[4];
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
@@ -568,7 +571,7 @@ __global__ void __launch_bounds__(kTcThreads) k_dense_3xtf32(float2* __restrict_
                     big[j] = to_tf32(v);
                     small[j] = to_tf32(__fsub_rn(v, __uint_as_float(big[j])));
                 }
-                const uint32_t off = tc::kmajor_offset(tid, kg * 4, KGA, 4);
+                const uint32_t off = tc::kmajor_offset(row, half * (RC / 2) + kg * 4, KGA, 4);
                 *reinterpret_cast<uint4*>(sAbig + off) = make_uint4(big[0], big[1], big[2], big[3]);
                 *reinterpret_cast<uint4*>(sAsmall + off) = make_uint4(small[0], small[1], small[2], small[3]);
             }
@@ -593,8 +596,8 @@ __global__ void __launch_bounds__(kTcThreads) k_dense_3xtf32(float2* __restrict_
             // the next chunk's amplitudes load while the tensor cores work on this one
             if (ch + 1 < KCH) {
 #pragma unroll
-                for (int c = 0; c < DC; c++)
-                    xv[c] = valid ? amps[base + p.off[(ch + 1) * DC + c]] : make_float2(0.f, 0.f);
+                for (int c = 0; c < DH; c++)
+                    xv[c] = valid ? amps[base + p.off[(ch + 1) * DC + half * DH + c]] : make_float2(0.f, 0.f);
             }
             const bool ok = tc::mbar_wait(&mbar, phase, kTcWaitLimit);
             phase ^= 1u;
@@ -606,15 +609,27 @@ __global__ void __launch_bounds__(kTcThreads) k_dense_3xtf32(float2* __restrict_
             tc::fence_after_sync();
         }
         if (timedOut) break;
-        const uint32_t lane = tmem + ((uint32_t)(warp * 32) << 16);
+        const uint32_t lane = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(half * HC);
+        if constexpr (HC >= 16) {
 #pragma unroll
-        for (int nc = 0; nc < R / 16; nc++) {
+            for (int nc = 0; nc < HC / 16; nc++) {
+                float v[16];
+                tc::ld16(lane + (uint32_t)(nc * 16), v);
+                tc::ld_wait();
+                if (valid) {
+#pragma unroll
+                    for (int j = 0; j < 8; j++)
+                        amps[base + p.off[half * (D / 2) + nc * 8 + j]] = make_float2(v[2 * j], v[2 * j + 1]);
+                }
+            }
+        } else {
             float v[16];
-            tc::ld16(lane + (uint32_t)(nc * 16), v);
+            tc::ld8(lane, v);
             tc::ld_wait();
             if (valid) {
 #pragma unroll
-                for (int j = 0; j < 8; j++) amps[base + p.off[nc * 8 + j]] = make_float2(v[2 * j], v[2 * j + 1]);
+                for (int j = 0; j < HC / 2; j++)
+                    amps[base + p.off[half * (D / 2) + j]] = make_float2(v[2 * j], v[2 * j + 1]);
             }
         }
         // every thread's TMEM reads of this tile precede the next tile's MMAs
@@ -761,7 +776,7 @@ static int dense_tc_run(State* s, const unsigned* targs, const double* g) {
     if (s->precision == DFS_C64) {
         auto kern = k_dense_3xtf32<IT, KT>;
         if ((rc = set_smem(kern, smem))) return rc;
-        kern<<<grid, kTcThreads, smem, ctx().stream>>>((float2*)s->amps, groups, p, (const uint4*)ctx().scratch);
+        kern<<<grid, 2 * kTcThreads, smem, ctx().stream>>>((float2*)s->amps, groups, p, (const uint4*)ctx().scratch);
     } else if constexpr (KT == 3) {
         // warp-specialised: two A buffers and two accumulator sets per CTA; shared memory
         // padded so that no more than kMinBlocks CTAs share an SM's 512 TMEM columns
