@@ -63,6 +63,8 @@ def parse():
                     help="comma-separated forms to run (adjoint, batched, precision32, fusion, dm12)")
     ap.add_argument("--form-scale", default="full", choices=["full", "small"],
                     help="small: the forms at reduced sizes, for profiling captures")
+    ap.add_argument("--batch-shape", default=None,
+                    help="CTAS_PER_SM,TEAM_WIDTH for the batched leg instead of autotuning")
     return ap.parse_args()
 
 
@@ -491,6 +493,9 @@ def batch_bytes(specs, circuits, elem):
     return total
 
 
+BATCH_SHAPE = None  # (CTAs per SM, team width) from --batch-shape
+
+
 def batch_leg(dfs, circuits, small=False):
     """One persistent launch (graph replay) for every circuit's <H> and gradient, against
     per-circuit runs through the circuit runtime."""
@@ -509,7 +514,10 @@ def batch_leg(dfs, circuits, small=False):
         b.setRandomStates(seed=STATE_SEED)
         b.setParams(np.concatenate(params))
         t0 = time.perf_counter()
-        b.autotune(gradient=True)
+        if BATCH_SHAPE:
+            b.setShape(*BATCH_SHAPE)
+        else:
+            b.autotune(gradient=True)
         tune_s = time.perf_counter() - t0
         b.run(gradient=True)
         runs = [_sync_time(dfs, lambda: b.run(gradient=True))[0] for _ in range(3)]
@@ -713,7 +721,10 @@ def cpu_baseline(args, circuits, gates):
 
 
 def main():
+    global BATCH_SHAPE
     args = parse()
+    if args.batch_shape:
+        BATCH_SHAPE = tuple(int(x) for x in args.batch_shape.split(","))
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         if rank != 0:
