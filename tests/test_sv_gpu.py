@@ -70,6 +70,20 @@ def test_many_targ(dfs, oracle, prec, k, rng):
                  lambda a: oracle.sv_many_targ(a, targs, g))
 
 
+@pytest.mark.parametrize("prec", ["c128"])
+def test_many_targ_3_tilings(dfs, oracle, prec, rng):
+    """Three targets on states of >= 10 qubits: the tensor-core kernel's tiles are 2^h
+    contiguous chunks of 2^(10-h) amplitudes, h = the targets at or above 10 - h; every
+    h, target order and the top and bottom qubits."""
+    cases = [(10, [0, 1, 2]), (10, [2, 9, 5]), (11, [9, 0, 10]), (12, [11, 3, 8]),
+             (12, [7, 8, 9]), (13, [12, 7, 0]), (13, [10, 11, 12]), (14, [13, 1, 9]),
+             (14, [6, 13, 2]), (15, [14, 0, 7]), (16, [8, 15, 9])]
+    for n, targs in cases:
+        g = haar(rng, 8)
+        run_pair(dfs, oracle, prec, n, rng, lambda s: dfs.distributed_statevector_manyTargGate(s, targs, g),
+                 lambda a: oracle.sv_many_targ(a, targs, g))
+
+
 @pytest.mark.parametrize("prec", PRECISIONS)
 def test_many_targ_whole_register(dfs, oracle, prec, rng):
     # all qubits targeted (the reference tests draw up to n targets on 6 qubits)
