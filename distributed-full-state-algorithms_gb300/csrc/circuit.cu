@@ -325,14 +325,15 @@ static std::vector<AdjTerm> make_terms(unsigned n, const double* coeffs, unsigne
 // each run of at least min_run operations is one pass of k_fused_run, every other
 // operation runs as its own kernel.  The plan depends only on the operations and the
 // precision.  Measured at 30 qubits: in complex64 a run costs about one HBM pass plus
-// ~1 ms of shared-memory work per operation (2.2x over separate kernels for runs of 18,
-// 1.07x for the random gate mix's runs of ~5); in complex128 the double-float arithmetic
-// of an operation in shared memory (~3.8 ms) nearly equals a separate HBM-bound kernel
-// (5.5 ms), so only long runs pay (1.25x at 12.5 operations, 0.7x at ~4).
+// ~1 ms of shared-memory work per operation (2.5x over separate kernels for runs of 40,
+// 1.08x for the random gate mix's runs of ~5); in complex128 the double-float arithmetic
+// of an operation in shared memory (~2.7 ms) is half a separate HBM-bound kernel
+// (5.3 ms): 1.72x for runs of 30, 1.02x for the gate mix's runs of >= 4 (runs of 3 lost,
+// 0.96x), and the 24-qubit gadget ansatz's forward and backward sweeps 13% and 6% faster.
 static size_t min_run(int precision, bool backward) {
     switch (precision) {
         case DFS_C64: return backward ? 2 : 3;  // a backward step moves twice the bytes
-        case DFS_C128: return 8;
+        case DFS_C128: return 4;
         default: return SIZE_MAX;  // native FP64 arithmetic is bound by the FP64 pipe either way
     }
 }

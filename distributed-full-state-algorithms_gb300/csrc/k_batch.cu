@@ -73,7 +73,7 @@ DEV bool team_sync(const Args& a, TeamSync* ts, unsigned& gen) {
 
 template <class P>
 DEV void forward_op(const Args& a, const OpD& op, typename P::store* x, IT N, Span sp, typename P::K* sG) {
-    apply_op<P>(op, a.mats, a.trig, x, N, sp, sG);
+    apply_op<P, span_unroll<P>(), true>(op, a.mats, a.trig, x, N, sp, sG);
 }
 
 template <class P>
@@ -96,8 +96,8 @@ DEV void backward_op(const Args& a, const OpD& op, typename P::store* x, typenam
         case BK_DENSE: {
             const int D2 = 1 << (2 * op.k);
             stage_gate<P>(a.mats + op.mat + 2 * D2, D2, sG);
-            op_dense_k<P>(op, x, N, sp, sG);
-            op_dense_k<P>(op, l, N, sp, sG);
+            op_dense_call<P>(op, x, N, sp, sG);
+            op_dense_call<P>(op, l, N, sp, sG);
             break;
         }
         case BK_GADGET: {
@@ -109,7 +109,7 @@ DEV void backward_op(const Args& a, const OpD& op, typename P::store* x, typenam
             }
             Sum s;
             sum_zero(s);
-            op_gadget_adj<P>(op, x, l, N, sp, c, sn, s);
+            op_gadget_adj_call<P>(op, x, l, N, sp, c, sn, s);
             s = block_reduce(s);
             if (threadIdx.x == 0) a.partials[(size_t)op.gradRow * a.width + rank] = sum_to_double2(s);
             break;
@@ -123,7 +123,7 @@ DEV void backward_op(const Args& a, const OpD& op, typename P::store* x, typenam
             }
             Sum s;
             sum_zero(s);
-            op_diag_adj<P>(op, x, l, N, sp, k0, k1, s);
+            op_diag_adj_call<P>(op, x, l, N, sp, k0, k1, s);
             s = block_reduce(s);
             if (threadIdx.x == 0) a.partials[(size_t)op.gradRow * a.width + rank] = sum_to_double2(s);
             break;
@@ -136,8 +136,9 @@ DEV void backward_op(const Args& a, const OpD& op, typename P::store* x, typenam
 }
 
 // lam <- H psi, partial sums of <psi|lam>
+// called, not inlined, for the same reason as the out-of-line operation forms
 template <class P>
-DEV void hamiltonian(const Args& a, const CircD& c, const typename P::store* x, typename P::store* l, IT N, Span sp,
+__device__ __noinline__ void hamiltonian(const Args& a, const CircD& c, const typename P::store* x, typename P::store* l, IT N, Span sp,
                      unsigned rank) {
     __shared__ AdjTerm sT[kMaxTerms];
     const unsigned T = c.termEnd - c.termBegin;

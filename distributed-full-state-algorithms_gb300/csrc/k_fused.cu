@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(kThreads) k_fused_run(typename P::store* __res
             PS::save(tile, l, P::load(amps, base + offLo[l & 63] + offHi[l >> 6]));
         __syncthreads();
         for (uint32_t o = 0; o < a.numOps; o++) {
-            batch::apply_op<PS>(a.ops[o], a.mats, a.trig, tile, T, sp, sG);
+            batch::apply_op<PS, 1, PS::kEmulated>(a.ops[o], a.mats, a.trig, tile, T, sp, sG);
             __syncthreads();
         }
         for (uint32_t l = threadIdx.x; l < T; l += kThreads)
@@ -69,30 +69,35 @@ DEV void bwd_op(const batch::OpD& op, const double* mats, const double2* trig, t
     switch (op.kind) {
         case batch::BK_PAIR:
             batch::stage_gate<PS>(mats + op.mat + 8, 4, sG);  // the adjoint follows the gate
-            batch::op_pair<PS>(op, x, T, sp, sG);
-            batch::op_pair<PS>(op, l, T, sp, sG);
+            batch::op_pair<PS, 1>(op, x, T, sp, sG);
+            batch::op_pair<PS, 1>(op, l, T, sp, sG);
             break;
         case batch::BK_SWAP:
-            batch::op_swap(op, x, T, sp);
-            batch::op_swap(op, l, T, sp);
+            batch::op_swap<typename PS::store, 1>(op, x, T, sp);
+            batch::op_swap<typename PS::store, 1>(op, l, T, sp);
             break;
         case batch::BK_DENSE: {
             const int D2 = 1 << (2 * op.k);
             batch::stage_gate<PS>(mats + op.mat + 2 * D2, D2, sG);
-            batch::op_dense_k<PS>(op, x, T, sp, sG);
-            batch::op_dense_k<PS>(op, l, T, sp, sG);
+            if constexpr (PS::kEmulated) {
+                batch::op_dense_call<PS>(op, x, T, sp, sG);
+                batch::op_dense_call<PS>(op, l, T, sp, sG);
+            } else {
+                batch::op_dense_k<PS>(op, x, T, sp, sG);
+                batch::op_dense_k<PS>(op, l, T, sp, sG);
+            }
             break;
         }
         case batch::BK_GADGET: {
             const typename PS::R c = PS::mkr(tr.x), sn = PS::mkr(-tr.y);
             if (op.gradRow < 0) {
-                batch::op_gadget<PS>(op, x, T, sp, c, sn);
-                batch::op_gadget<PS>(op, l, T, sp, c, sn);
+                batch::op_gadget<PS, 1>(op, x, T, sp, c, sn);
+                batch::op_gadget<PS, 1>(op, l, T, sp, c, sn);
                 break;
             }
             Sum s;
             sum_zero(s);
-            batch::op_gadget_adj<PS>(op, x, l, T, sp, c, sn, s);
+            batch::op_gadget_adj<PS, Sum, 1>(op, x, l, T, sp, c, sn, s);
             s = block_reduce(s);
             if (threadIdx.x == 0) sum_merge(sums[op.gradRow], s);
             break;
@@ -100,20 +105,20 @@ DEV void bwd_op(const batch::OpD& op, const double* mats, const double2* trig, t
         case batch::BK_DIAG: {
             const typename PS::K k0 = PS::mk(tr.x, -tr.y), k1 = PS::mk(tr.x, tr.y);
             if (op.gradRow < 0) {
-                batch::op_diag<PS>(op, x, T, sp, k0, k1);
-                batch::op_diag<PS>(op, l, T, sp, k0, k1);
+                batch::op_diag<PS, 1>(op, x, T, sp, k0, k1);
+                batch::op_diag<PS, 1>(op, l, T, sp, k0, k1);
                 break;
             }
             Sum s;
             sum_zero(s);
-            batch::op_diag_adj<PS>(op, x, l, T, sp, k0, k1, s);
+            batch::op_diag_adj<PS, Sum, 1>(op, x, l, T, sp, k0, k1, s);
             s = block_reduce(s);
             if (threadIdx.x == 0) sum_merge(sums[op.gradRow], s);
             break;
         }
         default:
-            batch::op_tensor(op, x, T, sp);
-            batch::op_tensor(op, l, T, sp);
+            batch::op_tensor<typename PS::store, 1>(op, x, T, sp);
+            batch::op_tensor<typename PS::store, 1>(op, l, T, sp);
             break;
     }
 }

@@ -42,6 +42,30 @@ DEV IT ins(IT j, const OpD& op) {
     return j;
 }
 
+// The items of a span, U at a time while a thread has U of them left: the U items'
+// loads are all issued before the first result is stored, which the compiler cannot do
+// by itself (the stores might alias the next loads); the rest one at a time.  `load(j)`
+// reads item j into a record, `store(j, r)` finishes it.
+template <int U, class Load, class Store>
+DEV void span_items(IT items, Span sp, Load load, Store store) {
+    IT j = sp.first;
+    if constexpr (U > 1) {
+        for (; j + (IT)(U - 1) * sp.stride < items; j += (IT)U * sp.stride) {
+            decltype(load(j)) r[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) r[u] = load(j + (IT)u * sp.stride);
+#pragma unroll
+            for (int u = 0; u < U; u++) store(j + (IT)u * sp.stride, r[u]);
+        }
+    }
+    for (; j < items; j += sp.stride) store(j, load(j));
+}
+
+// items per thread in flight: two for the double-float policy (four decoded amplitudes
+// per item would spill), four otherwise
+template <class P>
+constexpr int span_unroll() { return P::kEmulated ? 2 : 4; }
+
 template <class P>
 DEV void stage_gate(const double* m, int count, typename P::K* sG) {
     for (int e = threadIdx.x; e < count; e += kThreads) sG[e] = P::mk(m[2 * e], m[2 * e + 1]);
@@ -50,32 +74,54 @@ DEV void stage_gate(const double* m, int count, typename P::K* sG) {
 
 // ------------------------------------------------------------- operations
 
-template <class P>
+template <class P, int U = span_unroll<P>()>
 DEV void op_pair(const OpD& op, typename P::store* x, IT N, Span sp, const typename P::K* g) {
     const typename P::K g0 = g[0], g1 = g[1], g2 = g[2], g3 = g[3];
-    const IT items = N >> op.nq;
-    for (IT j = sp.first; j < items; j += sp.stride) {
-        IT i1 = ins(j, op) | op.setMask, i0 = i1 ^ op.tbit;
-        typename P::V x0 = P::load(x, i0), x1 = P::load(x, i1);
-        typename P::A a0 = P::first(g0, x0);
-        P::mac(a0, g1, x1);
-        typename P::A a1 = P::first(g2, x0);
-        P::mac(a1, g3, x1);
-        P::save(x, i0, P::get(a0));
-        P::save(x, i1, P::get(a1));
-    }
+    struct Rec {
+        IT i0, i1;
+        typename P::V x0, x1;
+    };
+    span_items<U>(
+        N >> op.nq, sp,
+        [&](IT j) {
+            Rec r;
+            r.i1 = ins(j, op) | op.setMask;
+            r.i0 = r.i1 ^ op.tbit;
+            r.x0 = P::load(x, r.i0);
+            r.x1 = P::load(x, r.i1);
+            return r;
+        },
+        [&](IT, const Rec& r) {
+            typename P::A a0 = P::first(g0, r.x0);
+            P::mac(a0, g1, r.x1);
+            typename P::A a1 = P::first(g2, r.x0);
+            P::mac(a1, g3, r.x1);
+            P::save(x, r.i0, P::get(a0));
+            P::save(x, r.i1, P::get(a1));
+        });
 }
 
-template <class S>
+template <class S, int U = sizeof(S) == 16 ? 2 : 4>
 DEV void op_swap(const OpD& op, S* x, IT N, Span sp) {
-    const IT items = N >> 2;
-    for (IT j = sp.first; j < items; j += sp.stride) {
-        IT b = ins(j, op);
-        IT i0 = b | op.setMask, i1 = b | op.tbit;
-        S t = x[i0];
-        x[i0] = x[i1];
-        x[i1] = t;
-    }
+    struct Rec {
+        IT i0, i1;
+        S a, b;
+    };
+    span_items<U>(
+        N >> 2, sp,
+        [&](IT j) {
+            Rec r;
+            const IT b = ins(j, op);
+            r.i0 = b | op.setMask;
+            r.i1 = b | op.tbit;
+            r.a = x[r.i0];
+            r.b = x[r.i1];
+            return r;
+        },
+        [&](IT, const Rec& r) {
+            x[r.i0] = r.b;
+            x[r.i1] = r.a;
+        });
 }
 
 template <class P, int K>
@@ -110,105 +156,172 @@ DEV void op_dense_k(const OpD& op, typename P::store* x, IT N, Span sp, const ty
 }
 
 // exp(i theta Q) with (c, sn) = (cos, sin) of +-theta; powY = (#Y + 1) mod 4
-template <class P>
+template <class P, int U = span_unroll<P>()>
 DEV void op_gadget(const OpD& op, typename P::store* x, IT N, Span sp, typename P::R c, typename P::R sn) {
-    const IT items = N >> 1;
-    for (IT j = sp.first; j < items; j += sp.stride) {
-        IT i0 = insert_zero(j, (int)op.top), i1 = i0 ^ op.maskX;
-        typename P::V x0 = P::load(x, i0), x1 = P::load(x, i1);
-        int s0 = parity(i0 & op.maskYZ), s1 = parity(i1 & op.maskYZ);
-        typename P::A a0 = P::first_r(c, x0);
-        P::mac_r(a0, sn, rot<P>(x1, op.powY, s1));
-        typename P::A a1 = P::first_r(c, x1);
-        P::mac_r(a1, sn, rot<P>(x0, op.powY, s0));
-        P::save(x, i0, P::get(a0));
-        P::save(x, i1, P::get(a1));
-    }
+    struct Rec {
+        IT i0, i1;
+        typename P::V x0, x1;
+    };
+    span_items<U>(
+        N >> 1, sp,
+        [&](IT j) {
+            Rec r;
+            r.i0 = insert_zero(j, (int)op.top);
+            r.i1 = r.i0 ^ op.maskX;
+            r.x0 = P::load(x, r.i0);
+            r.x1 = P::load(x, r.i1);
+            return r;
+        },
+        [&](IT, const Rec& r) {
+            const int s0 = parity(r.i0 & op.maskYZ), s1 = parity(r.i1 & op.maskYZ);
+            typename P::A a0 = P::first_r(c, r.x0);
+            P::mac_r(a0, sn, rot<P>(r.x1, op.powY, s1));
+            typename P::A a1 = P::first_r(c, r.x1);
+            P::mac_r(a1, sn, rot<P>(r.x0, op.powY, s0));
+            P::save(x, r.i0, P::get(a0));
+            P::save(x, r.i1, P::get(a1));
+        });
 }
 
-template <class P>
+template <class P, int U = span_unroll<P>()>
 DEV void op_diag(const OpD& op, typename P::store* x, IT N, Span sp, typename P::K k0, typename P::K k1) {
-    for (IT j = sp.first; j < N; j += sp.stride) {
-        typename P::V v = P::load(x, j);
-        P::save(x, j, P::mul(parity(j & op.maskYZ) ? k1 : k0, v));
-    }
+    span_items<U>(
+        N, sp, [&](IT j) { return P::load(x, j); },
+        [&](IT j, const typename P::V& v) { P::save(x, j, P::mul(parity(j & op.maskYZ) ? k1 : k0, v)); });
 }
 
-template <class S>
+template <class S, int U = sizeof(S) == 16 ? 2 : 4>
 DEV void op_tensor(const OpD& op, S* x, IT N, Span sp) {
     if (op.maskX == 0) {
-        for (IT j = sp.first; j < N; j += sp.stride)
-            if (parity(j & op.maskYZ)) x[j] = raw_neg(x[j]);
+        span_items<U>(
+            N, sp, [&](IT j) { return x[j]; },
+            [&](IT j, const S& v) {
+                if (parity(j & op.maskYZ)) x[j] = raw_neg(v);
+            });
         return;
     }
-    const IT items = N >> 1;
-    for (IT j = sp.first; j < items; j += sp.stride) {
-        IT i0 = insert_zero(j, (int)op.top), i1 = i0 ^ op.maskX;
-        S x0 = x[i0], x1 = x[i1];
-        x[i0] = raw_rot(x1, op.powY, parity(i1 & op.maskYZ));
-        x[i1] = raw_rot(x0, op.powY, parity(i0 & op.maskYZ));
-    }
+    struct Rec {
+        IT i0, i1;
+        S x0, x1;
+    };
+    span_items<U>(
+        N >> 1, sp,
+        [&](IT j) {
+            Rec r;
+            r.i0 = insert_zero(j, (int)op.top);
+            r.i1 = r.i0 ^ op.maskX;
+            r.x0 = x[r.i0];
+            r.x1 = x[r.i1];
+            return r;
+        },
+        [&](IT, const Rec& r) {
+            x[r.i0] = raw_rot(r.x1, op.powY, parity(r.i1 & op.maskYZ));
+            x[r.i1] = raw_rot(r.x0, op.powY, parity(r.i0 & op.maskYZ));
+        });
 }
 
 // fused adjoint step of a parametrised gadget: partial sums of
 // sum conj(l_j) (-1)^{par((j^X)&YZ)} x_{j^X}, then both <- exp(-i theta Q)
-template <class P, class Sum>
+template <class P, class Sum, int U = P::kEmulated ? 1 : 2>
 DEV void op_gadget_adj(const OpD& op, typename P::store* x, typename P::store* l, IT N, Span sp, typename P::R c,
                        typename P::R sn, Sum& s) {
-    const IT items = N >> 1;
-    for (IT j = sp.first; j < items; j += sp.stride) {
-        IT i0 = insert_zero(j, (int)op.top), i1 = i0 ^ op.maskX;
-        typename P::V x0 = P::load(x, i0), x1 = P::load(x, i1);
-        typename P::V l0 = P::load(l, i0), l1 = P::load(l, i1);
-        int s0 = parity(i0 & op.maskYZ), s1 = parity(i1 & op.maskYZ);
-        sum_add_conj_prod(s, l0, x1, s1);
-        sum_add_conj_prod(s, l1, x0, s0);
-        typename P::A a0 = P::first_r(c, x0);
-        P::mac_r(a0, sn, rot<P>(x1, op.powY, s1));
-        typename P::A a1 = P::first_r(c, x1);
-        P::mac_r(a1, sn, rot<P>(x0, op.powY, s0));
-        P::save(x, i0, P::get(a0));
-        P::save(x, i1, P::get(a1));
-        typename P::A b0 = P::first_r(c, l0);
-        P::mac_r(b0, sn, rot<P>(l1, op.powY, s1));
-        typename P::A b1 = P::first_r(c, l1);
-        P::mac_r(b1, sn, rot<P>(l0, op.powY, s0));
-        P::save(l, i0, P::get(b0));
-        P::save(l, i1, P::get(b1));
-    }
+    struct Rec {
+        IT i0, i1;
+        typename P::V x0, x1, l0, l1;
+    };
+    span_items<U>(
+        N >> 1, sp,
+        [&](IT j) {
+            Rec r;
+            r.i0 = insert_zero(j, (int)op.top);
+            r.i1 = r.i0 ^ op.maskX;
+            r.x0 = P::load(x, r.i0);
+            r.x1 = P::load(x, r.i1);
+            r.l0 = P::load(l, r.i0);
+            r.l1 = P::load(l, r.i1);
+            return r;
+        },
+        [&](IT, const Rec& r) {
+            const int s0 = parity(r.i0 & op.maskYZ), s1 = parity(r.i1 & op.maskYZ);
+            sum_add_conj_prod(s, r.l0, r.x1, s1);
+            sum_add_conj_prod(s, r.l1, r.x0, s0);
+            typename P::A a0 = P::first_r(c, r.x0);
+            P::mac_r(a0, sn, rot<P>(r.x1, op.powY, s1));
+            typename P::A a1 = P::first_r(c, r.x1);
+            P::mac_r(a1, sn, rot<P>(r.x0, op.powY, s0));
+            P::save(x, r.i0, P::get(a0));
+            P::save(x, r.i1, P::get(a1));
+            typename P::A b0 = P::first_r(c, r.l0);
+            P::mac_r(b0, sn, rot<P>(r.l1, op.powY, s1));
+            typename P::A b1 = P::first_r(c, r.l1);
+            P::mac_r(b1, sn, rot<P>(r.l0, op.powY, s0));
+            P::save(l, r.i0, P::get(b0));
+            P::save(l, r.i1, P::get(b1));
+        });
 }
 
-template <class P, class Sum>
+template <class P, class Sum, int U = P::kEmulated ? 2 : 4>
 DEV void op_diag_adj(const OpD& op, typename P::store* x, typename P::store* l, IT N, Span sp, typename P::K k0,
                      typename P::K k1, Sum& s) {
-    for (IT j = sp.first; j < N; j += sp.stride) {
-        typename P::V v = P::load(x, j), w = P::load(l, j);
-        int odd = parity(j & op.maskYZ);
-        sum_add_conj_prod(s, w, v, odd);
-        typename P::K k = odd ? k1 : k0;
-        P::save(x, j, P::mul(k, v));
-        P::save(l, j, P::mul(k, w));
-    }
+    struct Rec {
+        typename P::V v, w;
+    };
+    span_items<U>(
+        N, sp,
+        [&](IT j) {
+            Rec r;
+            r.v = P::load(x, j);
+            r.w = P::load(l, j);
+            return r;
+        },
+        [&](IT j, const Rec& r) {
+            const int odd = parity(j & op.maskYZ);
+            sum_add_conj_prod(s, r.w, r.v, odd);
+            const typename P::K k = odd ? k1 : k0;
+            P::save(x, j, P::mul(k, r.v));
+            P::save(l, j, P::mul(k, r.w));
+        });
+}
+
+// Out-of-line forms of the dense and adjoint steps for the persistent batched kernel:
+// called, not inlined, their register footprint (D amplitudes, or state and adjoint
+// pairs with a running sum) does not raise the rest of that kernel's allocation into
+// spills.  The fused-tile kernels inline them.
+template <class P>
+__device__ __noinline__ void op_dense_call(const OpD& op, typename P::store* x, IT N, Span sp,
+                                           const typename P::K* g) {
+    op_dense_k<P>(op, x, N, sp, g);
+}
+template <class P, class Sum>
+__device__ __noinline__ void op_gadget_adj_call(const OpD& op, typename P::store* x, typename P::store* l, IT N,
+                                                Span sp, typename P::R c, typename P::R sn, Sum& s) {
+    op_gadget_adj<P>(op, x, l, N, sp, c, sn, s);
+}
+template <class P, class Sum>
+__device__ __noinline__ void op_diag_adj_call(const OpD& op, typename P::store* x, typename P::store* l, IT N,
+                                              Span sp, typename P::K k0, typename P::K k1, Sum& s) {
+    op_diag_adj<P>(op, x, l, N, sp, k0, k1, s);
 }
 
 // the forward operation with its gate staged in shared memory and its (cos, sin) from trig
-template <class P>
+template <class P, int U = span_unroll<P>(), bool kCalled = false>
 DEV void apply_op(const OpD& op, const double* mats, const double2* trig, typename P::store* x, IT N, Span sp,
                   typename P::K* sG) {
     const double2 tr = trig[op.trig];
     switch (op.kind) {
         case BK_PAIR:
             stage_gate<P>(mats + op.mat, 4, sG);
-            op_pair<P>(op, x, N, sp, sG);
+            op_pair<P, U>(op, x, N, sp, sG);
             break;
-        case BK_SWAP: op_swap(op, x, N, sp); break;
+        case BK_SWAP: op_swap<typename P::store, U>(op, x, N, sp); break;
         case BK_DENSE:
             stage_gate<P>(mats + op.mat, 1 << (2 * op.k), sG);
-            op_dense_k<P>(op, x, N, sp, sG);
+            if constexpr (kCalled) op_dense_call<P>(op, x, N, sp, sG);
+            else op_dense_k<P>(op, x, N, sp, sG);
             break;
-        case BK_GADGET: op_gadget<P>(op, x, N, sp, P::mkr(tr.x), P::mkr(tr.y)); break;
-        case BK_DIAG: op_diag<P>(op, x, N, sp, P::mk(tr.x, tr.y), P::mk(tr.x, -tr.y)); break;
-        default: op_tensor(op, x, N, sp); break;
+        case BK_GADGET: op_gadget<P, U>(op, x, N, sp, P::mkr(tr.x), P::mkr(tr.y)); break;
+        case BK_DIAG: op_diag<P, U>(op, x, N, sp, P::mk(tr.x, tr.y), P::mk(tr.x, -tr.y)); break;
+        default: op_tensor<typename P::store, U>(op, x, N, sp); break;
     }
 }
 
