@@ -514,6 +514,281 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
     if (warp == 0) tc::tmem_free<2 * W::kAccCols>(tmem);
 }
 
+// ------------------------------------------ complex128, six targets (k = 6)
+// K = N = 128 reals: one tile in the other kernels' layout (128 groups x 6 slices of A,
+// and the 6 slices of B) would need 384 KB of shared memory, so the roles turn round.
+// The gate is the A operand (M = 128 output reals) and the state the B operand, N = 32
+// groups per tile: D[n][g] = sum_k G_R[n][k] X[g][k].  The gate's slices 0 and 1 sit in
+// TMEM (A read from tensor memory, 128 columns), slices 2..5 in shared memory (128 KB);
+// two sets of six accumulators of 32 columns take the other 384 columns, so that the MMAs
+// of one tile overlap the epilogue of the previous.
+// Digits: the 47-bit magnitudes are cut into a top byte (0..129) and five balanced bytes
+// (-128..127), one 64-bit addition of 0x8080808080 and a byte extraction.  A digit
+// product is then below 2^14, summed over K = 128 below 2^21, and the <= 6 products of one
+// weight below 2^24: each weight 2^0 .. 2^-40 has one exact FP32 accumulator.  (A
+// M = 128, K = 16 MMA costs at least ~44 cycles whatever N <= 32, ~70 at N = 64 and 128,
+// so the 168 MMAs of a tile are the bound: the tile is as wide as TMEM allows.)
+//   slicers (8 warps)   four groups per warp, 8 lanes per group, 8 amplitudes per lane
+//   MMA issuer (1 lane) the 21 digit products x 8 K steps of a tile
+//   epilogue (8 warps)  lane quadrant q of output reals, 16 of the 32 groups per warp
+// mbarriers as in k_dense_ozaki_ws (fullB, issued, mmaDone, accFree per buffer), every
+// wait bounded; one CTA per SM (it allocates all 512 TMEM columns).
+constexpr int kOz6Groups = 32;                                   // groups per tile (MMA N)
+constexpr int kOz6TmemSlices = 2;                                // gate slices held in TMEM
+constexpr int kOz6Accs = 6;
+constexpr uint32_t kOz6AccBase = 64 * kOz6TmemSlices;            // TMEM column of accumulator set 0
+constexpr uint32_t kOz6AccSet = kOz6Accs * kOz6Groups;           // columns of one set
+constexpr uint32_t kOz6BSlice = kOz6Groups * 128 * 2;            // one state slice (8 KB)
+constexpr uint32_t kOz6BBuf = kOzSlices * kOz6BSlice;            // one tile's six slices
+constexpr uint32_t kOz6ASlice = 128 * 128 * 2;                   // one gate slice (32 KB)
+constexpr uint32_t kOz6TmemWords = kOz6TmemSlices * 128 * 64;    // packed gate slices in TMEM
+constexpr int kOz6Threads = 8 * 32 + 8 * 32 + 32;
+constexpr uint64_t kOz6Bias = 0x8080808080ull;                   // +128 on the five low bytes
+static_assert(kOz6AccBase + 2 * kOz6AccSet <= 512, "TMEM budget");
+
+// the 47-bit magnitude of a double relative to 2^(E - 1022), E the group's largest exponent
+DEV uint64_t fraction47(uint32_t H, uint32_t L, uint32_t E) {
+    uint32_t ex = (H >> 20) & 0x7FFu;
+    uint64_t M = ((uint64_t)((H & 0xFFFFFu) | 0x100000u) << 32) | L;
+    uint32_t sh = E - ex + 6u;
+    uint64_t F = sh < 64u ? (M >> sh) : 0ull;
+    return ex == 0u ? 0ull : F;
+}
+
+template <class IT>
+__global__ void __launch_bounds__(kOz6Threads, 1)
+    k_dense_ozaki6(uint4* __restrict__ amps, IT numGroups, DenseParams<IT, 6> p, const uint32_t* __restrict__ gsl) {
+    constexpr uint32_t KG = 16;  // core matrices along K
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* sA = smem;                                                // gate slices 2..5
+    unsigned char* sB = smem + (kOzSlices - kOz6TmemSlices) * kOz6ASlice;   // two tiles of state slices
+    __shared__ __align__(8) uint64_t fullB[2], issued[2], mmaDone[2], accFree[2], drain;
+    __shared__ uint32_t tmemSlot;
+    __shared__ uint32_t sE[2][kOz6Groups];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(gsl + kOz6TmemWords);
+        for (int i = tid; i < (int)((kOzSlices - kOz6TmemSlices) * kOz6ASlice / 16); i += kOz6Threads)
+            reinterpret_cast<uint4*>(sA)[i] = src[i];
+    }
+    if (warp == 0) tc::tmem_alloc<512>(&tmemSlot);
+    if (tid == 0) {
+        for (int b = 0; b < 2; b++) {
+            tc::mbar_init(&fullB[b], 256);
+            tc::mbar_init(&issued[b], 1);
+            tc::mbar_init(&mmaDone[b], 1);
+            tc::mbar_init(&accFree[b], 256);
+        }
+        tc::mbar_init(&drain, 1);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tmemSlot;
+    // gate slices 0 and 1 into TMEM: warp 8 + q writes lanes 32q .. 32q + 31 (output reals)
+    if (warp >= 8 && warp < 12) {
+        const int m = (warp & 3) * 32 + lane;
+        for (int s = 0; s < kOz6TmemSlices; s++)
+            for (int i = 0; i < 4; i++) {
+                uint32_t v[16];
+#pragma unroll
+                for (int e = 0; e < 16; e++) v[e] = gsl[(s * 128 + m) * 64 + i * 16 + e];
+                tc::st16(tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(s * 64 + i * 16), v);
+            }
+        tc::st_wait();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+
+    const IT numTiles = (numGroups + kOz6Groups - 1) / kOz6Groups;
+    const int myTiles = (IT)blockIdx.x < numTiles ? (int)((numTiles - 1 - (IT)blockIdx.x) / gridDim.x) + 1 : 0;
+    bool ok = true;
+
+    if (warp < 8) {
+        // ---- slicers: group 4 * warp + (lane >> 3) of the tile, amplitudes 8 * (lane & 7) + j
+        constexpr int H = 8;
+        const int gl = warp * 4 + (lane >> 3), part = lane & 7;
+        auto load = [&](int i, uint4 (&v)[H]) {
+            const IT g = ((IT)blockIdx.x + (IT)i * gridDim.x) * kOz6Groups + (IT)gl;
+            const bool in = i < myTiles && g < numGroups;
+            const IT b = in ? insert_zeros(g, p.q) : (IT)0;
+#pragma unroll
+            for (int c = 0; c < H; c++) v[c] = in ? amps[b + p.off[part * H + c]] : make_uint4(0, 0, 0, 0);
+        };
+        uint4 cur[H], nxt[H];
+        load(0, cur);
+        for (int i = 0; i < myTiles; i++) {
+            const int b = i & 1;
+            const uint32_t k = (uint32_t)i >> 1;
+            load(i + 1, nxt);
+            if (i >= 2 && !(ok = tc::mbar_wait(&accFree[b], (k - 1) & 1, kTcWaitLimit))) break;
+            uint32_t E = 0;
+#pragma unroll
+            for (int c = 0; c < H; c++) E = max(E, max((cur[c].y >> 20) & 0x7FFu, (cur[c].w >> 20) & 0x7FFu));
+#pragma unroll
+            for (int m = 4; m >= 1; m >>= 1) E = max(E, __shfl_xor_sync(0xffffffffu, E, m));
+            if (part == 0) sE[b][gl] = E;
+#pragma unroll
+            for (int half = 0; half < 2; half++) {
+                uint32_t packed[kOzSlices][4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const uint4 v = cur[half * 4 + j];
+                    const uint64_t G0 = fraction47(v.y, v.x, E) + kOz6Bias, G1 = fraction47(v.w, v.z, E) + kOz6Bias;
+                    const uint32_t Gh0 = (uint32_t)(G0 >> 32), Gl0 = (uint32_t)G0;
+                    const uint32_t Gh1 = (uint32_t)(G1 >> 32), Gl1 = (uint32_t)G1;
+                    const uint32_t mb0 = (v.y >> 31) ? 0xCB000000u : 0x4B000000u;
+                    const uint32_t mb1 = (v.w >> 31) ? 0xCB000000u : 0x4B000000u;
+                    // top digit: +-(2^23 + byte) - +-2^23; low digits: - +-(2^23 + 128)
+                    const uint64_t magicTop = tc::pk2(__uint_as_float(mb0), __uint_as_float(mb1));
+                    const uint64_t magicLow = tc::pk2(__uint_as_float(mb0 | 0x80u), __uint_as_float(mb1 | 0x80u));
+                    uint32_t m0[kOzSlices], m1[kOzSlices];
+                    m0[0] = __byte_perm(Gh0, mb0, 0x7651u);
+                    m0[1] = __byte_perm(Gh0, mb0, 0x7650u);
+                    m0[2] = __byte_perm(Gl0, mb0, 0x7653u);
+                    m0[3] = __byte_perm(Gl0, mb0, 0x7652u);
+                    m0[4] = __byte_perm(Gl0, mb0, 0x7651u);
+                    m0[5] = __byte_perm(Gl0, mb0, 0x7650u);
+                    m1[0] = __byte_perm(Gh1, mb1, 0x7651u);
+                    m1[1] = __byte_perm(Gh1, mb1, 0x7650u);
+                    m1[2] = __byte_perm(Gl1, mb1, 0x7653u);
+                    m1[3] = __byte_perm(Gl1, mb1, 0x7652u);
+                    m1[4] = __byte_perm(Gl1, mb1, 0x7651u);
+                    m1[5] = __byte_perm(Gl1, mb1, 0x7650u);
+#pragma unroll
+                    for (int sl = 0; sl < kOzSlices; sl++) {
+                        float re, im;
+                        tc::up2(tc::sub2(tc::pk2(__uint_as_float(m0[sl]), __uint_as_float(m1[sl])),
+                                         sl == 0 ? magicTop : magicLow),
+                                re, im);
+                        packed[sl][j] = pack_bf16(re, im);
+                    }
+                }
+                // these 4 amplitudes' 8 reals are one 16-byte core row of each slice
+                unsigned char* dst = sB + b * kOz6BBuf + tc::kmajor_offset(gl, part * 16 + half * 8, KG, 2);
+#pragma unroll
+                for (int sl = 0; sl < kOzSlices; sl++)
+                    *reinterpret_cast<uint4*>(dst + sl * kOz6BSlice) =
+                        make_uint4(packed[sl][0], packed[sl][1], packed[sl][2], packed[sl][3]);
+            }
+            tc::fence_smem_to_async();
+            tc::mbar_arrive(&fullB[b]);
+#pragma unroll
+            for (int c = 0; c < H; c++) cur[c] = nxt[c];
+        }
+    } else if (warp < 16) {
+        // ---- epilogue: output real n = 32 q + lane of 16 groups (half gh of the tile)
+        const int q = warp & 3, gh = (warp - 8) >> 2;
+        const int n = q * 32 + lane;
+        const int colExp = p.colExp[n];
+        const IT off = p.off[n >> 1];
+        uint2* out = reinterpret_cast<uint2*>(amps);
+        for (int i = 0; i < myTiles; i++) {
+            const int b = i & 1;
+            const uint32_t k = (uint32_t)i >> 1;
+            if (!(ok = tc::mbar_wait(&issued[b], k & 1, kTcWaitLimit) && tc::mbar_wait(&mmaDone[b], k & 1, kTcWaitLimit)))
+                break;
+            tc::fence_after_sync();
+            const IT gt = ((IT)blockIdx.x + (IT)i * gridDim.x) * kOz6Groups;
+#pragma unroll 1
+            for (int ch = 0; ch < 2; ch++) {
+                const int gc = gh * 16 + ch * 8;  // the chunk's first group in the tile
+                uint32_t E[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++) E[j] = sE[b][gc + j];
+                float acc[kOz6Accs][8];
+                const uint32_t lanes =
+                    tmem + ((uint32_t)(q * 32) << 16) + kOz6AccBase + (uint32_t)b * kOz6AccSet + (uint32_t)gc;
+#pragma unroll
+                for (int u = 0; u < kOz6Accs; u++) {
+                    float v[16];
+                    tc::ld8(lanes + (uint32_t)(u * kOz6Groups), v);
+#pragma unroll
+                    for (int j = 0; j < 8; j++) acc[u][j] = v[j];
+                }
+                tc::ld_wait();
+#pragma unroll
+                for (int j2 = 0; j2 < 4; j2++) {
+                    // two groups as an f32x2 pair; y = sum_u D_u 2^-8u, the first three exactly
+                    uint64_t a[kOz6Accs];
+#pragma unroll
+                    for (int u = 0; u < kOz6Accs; u++) a[u] = tc::pk2(acc[u][2 * j2], acc[u][2 * j2 + 1]);
+                    uint64_t t, e, e1;
+                    tc::two_sum2(a[0], tc::mul2(a[1], tc::pk2(0x1p-8f, 0x1p-8f)), t, e);
+                    tc::two_sum2(t, tc::mul2(a[2], tc::pk2(0x1p-16f, 0x1p-16f)), t, e1);
+                    e = tc::add2(e, e1);
+                    e = tc::fma2(a[3], tc::pk2(0x1p-24f, 0x1p-24f), e);
+                    e = tc::fma2(a[4], tc::pk2(0x1p-32f, 0x1p-32f), e);
+                    e = tc::fma2(a[5], tc::pk2(0x1p-40f, 0x1p-40f), e);
+                    uint64_t y, yl;
+                    tc::fast_two_sum2(t, e, y, yl);
+                    df::f2 y0, y1;
+                    tc::up2(y, y0.hi, y1.hi);
+                    tc::up2(yl, y0.lo, y1.lo);
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const int j = 2 * j2 + h;
+                        const IT g = gt + (IT)(gc + j);
+                        if (g < numGroups) {
+                            uint32_t w[2];
+                            df::encode_words_scaled(h ? y1 : y0, (int)E[j] + colExp - 1036, &w[1], &w[0]);
+                            out[2 * (insert_zeros(g, p.q) + off) + (n & 1)] = make_uint2(w[0], w[1]);
+                        }
+                    }
+                }
+            }
+            tc::fence_before_sync();
+            tc::mbar_arrive(&accFree[b]);
+        }
+    } else if (lane == 0) {
+        // ---- MMA issuer: digit products (s, t), s + t <= 5, into accumulator s + t
+        const uint32_t id = tc::idesc(1, kOz6Groups);
+        int issuedTiles = 0;
+        for (int i = 0; i < myTiles; i++) {
+            const int b = i & 1;
+            const uint32_t k = (uint32_t)i >> 1;
+            if (!(ok = tc::mbar_wait(&fullB[b], k & 1, kTcWaitLimit))) break;
+            if (i >= 2 && !(ok = tc::mbar_wait(&accFree[b], (k - 1) & 1, kTcWaitLimit))) break;
+            tc::fence_after_sync();
+            const uint32_t dst = tmem + kOz6AccBase + (uint32_t)b * kOz6AccSet;
+            // descriptors advance by (byte offset >> 4) in their address field
+            const uint64_t dB = tc::desc(tc::smem_u32(sB + b * kOz6BBuf), 128, 128 * KG);
+            const uint64_t dA = tc::desc(tc::smem_u32(sA), 128, 128 * KG);
+#pragma unroll
+            for (int ks = 0; ks < 8; ks++) {
+#pragma unroll
+                for (int s = 0; s < kOzSlices; s++) {
+#pragma unroll
+                    for (int t = 0; t + s < kOzSlices; t++) {
+                        const uint64_t db = dB + (uint64_t)((t * kOz6BSlice + ks * 256) >> 4);
+                        const uint32_t d = dst + (uint32_t)((s + t) * kOz6Groups);
+                        // the first product into accumulator u is (0, u) at K step 0
+                        const uint32_t accum = (ks == 0 && s == 0) ? 0u : 1u;
+                        if (s < kOz6TmemSlices)
+                            tc::mma_bf16_ts(d, tmem + (uint32_t)(s * 64 + ks * 8), db, id, accum);
+                        else
+                            tc::mma_bf16(d, dA + (uint64_t)(((s - kOz6TmemSlices) * kOz6ASlice + ks * 256) >> 4), db,
+                                         id, accum);
+                    }
+                }
+            }
+            tc::commit(&mmaDone[b]);
+            tc::mbar_arrive(&issued[b]);
+            issuedTiles++;
+        }
+        if (issuedTiles > 0) {
+            tc::commit(&drain);
+            if (!tc::mbar_wait(&drain, 0, kTcWaitLimit)) ok = false;
+        }
+    }
+    if (!ok) atomicExch(&g_tcTimeout, 1);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_free<512>(tmem);
+}
+
 // ------------------------------------------------------------- complex64
 
 DEV uint32_t to_tf32(float x) {
@@ -690,6 +965,50 @@ static void prepare_ozaki_b(const double* g, std::vector<unsigned char>& bytes, 
     }
 }
 
+// the six-target complex128 gate: 47-bit magnitudes in the digits of k_dense_ozaki6 (a
+// top byte, five balanced bytes); slices 0 and 1 packed for TMEM ([slice][row][K / 2], two
+// bf16 per word, the lower K in the low half), slices 2..5 in the K-major shared-memory
+// layout; colExp[n] the power of two of gate row n, as in prepare_ozaki_b
+static void prepare_ozaki6(const double* g, std::vector<unsigned char>& bytes, int* colExp) {
+    constexpr int D = 64, R = 128;
+    bytes.assign(kOz6TmemWords * 4 + (kOzSlices - kOz6TmemSlices) * kOz6ASlice, 0);
+    for (int n = 0; n < R; n++) {
+        int F = 0;
+        bool any = false;
+        for (int kk = 0; kk < R; kk++) {
+            double v = real_form(g, D, n, kk);
+            if (v != 0.0) {
+                int e;
+                std::frexp(v, &e);
+                F = any ? std::max(F, e) : e;
+                any = true;
+            }
+        }
+        colExp[n] = F;
+        for (int kk = 0; kk < R; kk++) {
+            double v = real_form(g, D, n, kk);
+            const uint64_t V = (uint64_t)std::ldexp(std::fabs(v), 47 - F);  // < 2^47, exact floor
+            const uint64_t Gb = V + kOz6Bias;
+            const double sign = v < 0 ? -1.0 : 1.0;
+            for (int t = 0; t < kOzSlices; t++) {
+                const int byte = (int)((Gb >> (8 * (kOzSlices - 1 - t))) & 0xFF);
+                const int digit = t == 0 ? byte : byte - 128;
+                float f = (float)(sign * digit);  // |digit| <= 129: exact in bf16
+                uint32_t fb;
+                std::memcpy(&fb, &f, 4);
+                const uint16_t h = (uint16_t)(fb >> 16);
+                size_t off;
+                if (t < kOz6TmemSlices)
+                    off = ((size_t)(t * 128 + n) * 64 + kk / 2) * 4 + (kk & 1) * 2;
+                else
+                    off = (size_t)kOz6TmemWords * 4 + (size_t)(t - kOz6TmemSlices) * kOz6ASlice +
+                          tc::kmajor_offset(n, kk, 16, 2);
+                std::memcpy(&bytes[off], &h, 2);
+            }
+        }
+    }
+}
+
 static uint32_t host_tf32(float x) {
     uint32_t b;
     std::memcpy(&b, &x, 4);
@@ -738,8 +1057,28 @@ static int set_smem(K kernel, size_t bytes) {
     return e == cudaSuccess ? DFS_SUCCESS : cuda_fail(e, "cudaFuncSetAttribute(dense)");
 }
 
+// complex128, six targets: one CTA per SM (all 512 TMEM columns), 224 KB of shared memory
+template <class IT>
+static int launch_ozaki6(State* s, const unsigned* targs, const double* g) {
+    const IT groups = (IT)(s->numAmps >> 6);
+    DenseParams<IT, 6> p = dense_params<IT, 6>(targs);
+    std::vector<unsigned char> bytes;
+    prepare_ozaki6(g, bytes, p.colExp);
+    int rc = upload_scratch(bytes.data(), bytes.size(), 0);
+    if (rc) return rc;
+    const size_t smem = (kOzSlices - kOz6TmemSlices) * kOz6ASlice + 2 * kOz6BBuf;
+    auto kern = k_dense_ozaki6<IT>;
+    if ((rc = set_smem(kern, smem))) return rc;
+    const uint64_t tiles = ((uint64_t)groups + kOz6Groups - 1) / kOz6Groups;
+    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(tiles, (uint64_t)ctx().numSMs));
+    kern<<<grid, kOz6Threads, smem, ctx().stream>>>((uint4*)s->amps, groups, p, (const uint32_t*)ctx().scratch);
+    return check_launch("manyTargGate (tensor cores, 6 targets)");
+}
+
 template <class IT, int KT>
 static int dense_tc_run(State* s, const unsigned* targs, const double* g) {
+    if constexpr (KT == 6)
+        if (s->precision != DFS_C64) return launch_ozaki6<IT>(s, targs, g);
     using S = Dense<KT>;
     const IT groups = (IT)(s->numAmps >> KT);
     const uint64_t tiles = (groups + 127) / 128;
@@ -806,7 +1145,7 @@ static int dense_tc_run(State* s, const unsigned* targs, const double* g) {
 bool dense_tc_supported(const State* s, unsigned k) {
     if (s->precision == DFS_C128_NATIVE || !ctx().denseTensorCores) return false;
     if (s->precision == DFS_C64) return k >= 4 && k <= 6;
-    return k >= 3 && k <= 5;
+    return k >= 3 && k <= 6;
 }
 
 int dense_tc(State* s, const unsigned* targs, unsigned k, const double* gate) {
@@ -815,9 +1154,7 @@ int dense_tc(State* s, const unsigned* targs, unsigned k, const double* gate) {
         case 3: return wide ? dense_tc_run<uint64_t, 3>(s, targs, gate) : dense_tc_run<uint32_t, 3>(s, targs, gate);
         case 4: return wide ? dense_tc_run<uint64_t, 4>(s, targs, gate) : dense_tc_run<uint32_t, 4>(s, targs, gate);
         case 5: return wide ? dense_tc_run<uint64_t, 5>(s, targs, gate) : dense_tc_run<uint32_t, 5>(s, targs, gate);
-        case 6:
-            if (s->precision != DFS_C64) break;
-            return wide ? dense_tc_run<uint64_t, 6>(s, targs, gate) : dense_tc_run<uint32_t, 6>(s, targs, gate);
+        case 6: return wide ? dense_tc_run<uint64_t, 6>(s, targs, gate) : dense_tc_run<uint32_t, 6>(s, targs, gate);
         default: break;
     }
     return fail(DFS_ERR_INVALID_ARG, "no tensor-core path for %u targets", k);

@@ -41,6 +41,15 @@ DEV void mma_tf32(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t id, uint32_t 
         "l"(a), "l"(b), "r"(id), "r"(accumulate));
 }
 
+// the same with the A operand in TMEM (row m of A in lane m, two 16-bit elements of K
+// per 32-bit column, the lower K in the low half)
+DEV void mma_bf16_ts(uint32_t dtmem, uint32_t atmem, uint64_t b, uint32_t id, uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}" ::"r"(dtmem),
+        "r"(atmem), "l"(b), "r"(id), "r"(accumulate));
+}
+
 // arrive on `mbar` when every MMA this thread issued so far has completed
 DEV void commit(uint64_t* mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar)));
@@ -101,6 +110,17 @@ DEV void ld8(uint32_t taddr, float (&v)[16]) {
                  : "r"(taddr));
 }
 DEV void ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// 16 consecutive 32-bit columns of this thread's TMEM lane (the warp's 32 lanes) from registers
+DEV void st16(uint32_t taddr, const uint32_t (&v)[16]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+            taddr),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]),
+        "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
+        : "memory");
+}
+DEV void st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // packed float pairs (df::pk2 ...) for the epilogues
 using df::add2;

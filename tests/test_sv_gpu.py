@@ -84,6 +84,18 @@ def test_many_targ_3_tilings(dfs, oracle, prec, rng):
                  lambda a: oracle.sv_many_targ(a, targs, g))
 
 
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+def test_many_targ_6_many_tiles(dfs, oracle, prec, rng):
+    """Six targets on states of many 16-group tiles (the complex128 kernel's tiles; the
+    complex64 kernel's are 128 groups): low, high, scattered and unsorted targets."""
+    cases = [(12, [0, 1, 2, 3, 4, 5]), (14, [13, 12, 11, 10, 9, 8]), (16, [15, 0, 7, 3, 11, 5]),
+             (17, [2, 16, 9, 4, 13, 6])]
+    for n, targs in cases:
+        g = haar(rng, 64)
+        run_pair(dfs, oracle, prec, n, rng, lambda s: dfs.distributed_statevector_manyTargGate(s, targs, g),
+                 lambda a: oracle.sv_many_targ(a, targs, g))
+
+
 @pytest.mark.parametrize("prec", PRECISIONS)
 def test_many_targ_whole_register(dfs, oracle, prec, rng):
     # all qubits targeted (the reference tests draw up to n targets on 6 qubits)
