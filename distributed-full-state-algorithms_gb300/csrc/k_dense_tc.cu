@@ -565,6 +565,7 @@ __global__ void __launch_bounds__(kOz6Threads, 1)
     __shared__ __align__(8) uint64_t fullB[2], issued[2], mmaDone[2], accFree[2], drain;
     __shared__ uint32_t tmemSlot;
     __shared__ uint32_t sE[2][kOz6Groups];
+    __shared__ IT sBase[2][kOz6Groups];  // amplitude index of each group's first amplitude
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     {
@@ -610,26 +611,30 @@ __global__ void __launch_bounds__(kOz6Threads, 1)
         // ---- slicers: group 4 * warp + (lane >> 3) of the tile, amplitudes 8 * (lane & 7) + j
         constexpr int H = 8;
         const int gl = warp * 4 + (lane >> 3), part = lane & 7;
-        auto load = [&](int i, uint4 (&v)[H]) {
+        IT curBase = 0, nxtBase = 0;
+        auto load = [&](int i, uint4 (&v)[H], IT& base) {
             const IT g = ((IT)blockIdx.x + (IT)i * gridDim.x) * kOz6Groups + (IT)gl;
             const bool in = i < myTiles && g < numGroups;
-            const IT b = in ? insert_zeros(g, p.q) : (IT)0;
+            base = in ? insert_zeros(g, p.q) : (IT)0;
 #pragma unroll
-            for (int c = 0; c < H; c++) v[c] = in ? amps[b + p.off[part * H + c]] : make_uint4(0, 0, 0, 0);
+            for (int c = 0; c < H; c++) v[c] = in ? amps[base + p.off[part * H + c]] : make_uint4(0, 0, 0, 0);
         };
         uint4 cur[H], nxt[H];
-        load(0, cur);
+        load(0, cur, curBase);
         for (int i = 0; i < myTiles; i++) {
             const int b = i & 1;
             const uint32_t k = (uint32_t)i >> 1;
-            load(i + 1, nxt);
+            load(i + 1, nxt, nxtBase);
             if (i >= 2 && !(ok = tc::mbar_wait(&accFree[b], (k - 1) & 1, kTcWaitLimit))) break;
             uint32_t E = 0;
 #pragma unroll
             for (int c = 0; c < H; c++) E = max(E, max((cur[c].y >> 20) & 0x7FFu, (cur[c].w >> 20) & 0x7FFu));
 #pragma unroll
             for (int m = 4; m >= 1; m >>= 1) E = max(E, __shfl_xor_sync(0xffffffffu, E, m));
-            if (part == 0) sE[b][gl] = E;
+            if (part == 0) {
+                sE[b][gl] = E;
+                sBase[b][gl] = curBase;
+            }
 #pragma unroll
             for (int half = 0; half < 2; half++) {
                 uint32_t packed[kOzSlices][4];
@@ -677,6 +682,7 @@ __global__ void __launch_bounds__(kOz6Threads, 1)
             tc::mbar_arrive(&fullB[b]);
 #pragma unroll
             for (int c = 0; c < H; c++) cur[c] = nxt[c];
+            curBase = nxtBase;
         }
     } else if (warp < 16) {
         // ---- epilogue: output real n = 32 q + lane of 16 groups (half gh of the tile)
@@ -696,8 +702,12 @@ __global__ void __launch_bounds__(kOz6Threads, 1)
             for (int ch = 0; ch < 2; ch++) {
                 const int gc = gh * 16 + ch * 8;  // the chunk's first group in the tile
                 uint32_t E[8];
+                IT base[8];
 #pragma unroll
-                for (int j = 0; j < 8; j++) E[j] = sE[b][gc + j];
+                for (int j = 0; j < 8; j++) {
+                    E[j] = sE[b][gc + j];
+                    base[j] = sBase[b][gc + j];
+                }
                 float acc[kOz6Accs][8];
                 const uint32_t lanes =
                     tmem + ((uint32_t)(q * 32) << 16) + kOz6AccBase + (uint32_t)b * kOz6AccSet + (uint32_t)gc;
@@ -734,7 +744,7 @@ __global__ void __launch_bounds__(kOz6Threads, 1)
                         if (g < numGroups) {
                             uint32_t w[2];
                             df::encode_words_scaled(h ? y1 : y0, (int)E[j] + colExp - 1036, &w[1], &w[0]);
-                            out[2 * (insert_zeros(g, p.q) + off) + (n & 1)] = make_uint2(w[0], w[1]);
+                            out[2 * (base[j] + off) + (n & 1)] = make_uint2(w[0], w[1]);
                         }
                     }
                 }
