@@ -1148,10 +1148,9 @@ static int dense_tc_run(State* s, const unsigned* targs, const double* g) {
     return check_launch("manyTargGate (tensor cores)");
 }
 
-// measured at 30 qubits: complex128 k=3 3.4 TB/s (CUDA cores 2.4), k=4 3.2 (0.75);
-// complex64 k=4 5.2 TB/s (0.9), while k=3 stays on the FP32 CUDA cores (6.0 vs 4.9).
-// k = 5 (both) and k = 6 (complex64, A staged in two K halves) follow the same kernels;
-// complex128 k = 6 would need 192 KB of A slices and 393 KB of B slices per tile.
+// measured at 30 qubits (ms per gate, tensor cores / CUDA cores): complex128 k = 3 8.2 /
+// 14.3, k = 4 9.8 / 46, k = 5 12.2, k = 6 18.1 / 146; complex64 k = 4 3.17 / 19, k = 5 5.05,
+// k = 6 5.55, while complex64 k = 3 stays on the FP32 CUDA cores (6.0 vs 4.9 TB/s).
 bool dense_tc_supported(const State* s, unsigned k) {
     if (s->precision == DFS_C128_NATIVE || !ctx().denseTensorCores) return false;
     if (s->precision == DFS_C64) return k >= 4 && k <= 6;
