@@ -10,5 +10,7 @@ from .api import *  # noqa: F401,F403
 from .api import __all__ as _api_all
 from ._lib import C128, C128_NATIVE, C64, DfsError, load as load_library
 from .circuit import Batch, Circuit, expectation
+from . import state_file
 
-__all__ = list(_api_all) + ["C128", "C128_NATIVE", "C64", "load_library", "Circuit", "Batch", "expectation"]
+__all__ = list(_api_all) + ["C128", "C128_NATIVE", "C64", "load_library", "Circuit", "Batch", "expectation",
+                            "state_file"]

@@ -29,6 +29,7 @@ ERRORS = {
     8: "not initialised",
     9: "precision mismatch",
     10: "device wait timed out",
+    11: "state file error",
 }
 
 
@@ -84,6 +85,8 @@ PROTOTYPES = {
     "dfs_state_set_zero": [_H],
     "dfs_state_set_classical": [_H, _U64],
     "dfs_state_set_random": [_H, _U64, _I],
+    "dfs_state_save": [_H, C.c_char_p],
+    "dfs_state_load": [C.c_char_p, _HP],
     "dfs_statevector_oneTargGate": [_H, _U, _DP],
     "dfs_statevector_manyCtrlOneTargGate": [_H, _UP, _U, _U, _DP],
     "dfs_statevector_swapGate": [_H, _U, _U],

@@ -14,6 +14,7 @@ assertions raise :class:`DfsError`.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from typing import Sequence
 
 import numpy as np
@@ -23,7 +24,7 @@ from ._lib import DfsError, StateInfo, call
 
 __all__ = [
     "DfsError", "StateVector", "DensityMatrix", "comm_init", "comm_end", "comm_getRank", "comm_getNumNodes",
-    "comm_synch", "set_stream",
+    "comm_synch", "set_stream", "load",
     "distributed_statevector_oneTargGate", "distributed_statevector_manyCtrlOneTargGate",
     "distributed_statevector_swapGate", "distributed_statevector_manyTargGate",
     "distributed_statevector_pauliTensor", "distributed_statevector_pauliGadget",
@@ -160,6 +161,11 @@ class StateVector:
         call("dfs_state_device_ptr", self._h, C.byref(p))
         return p.value or 0
 
+    def save(self, path) -> None:
+        """Write the state to a file (``dfs_state_save``; the layout is in
+        ``state_file.py``)."""
+        call("dfs_state_save", self._h, os.fsencode(path))
+
     def printAmps(self) -> None:
         print(f"rank {self.rank}:")
         print("{" + " ".join(str(a) for a in self.getAllVecAmps()) + "}")
@@ -193,6 +199,16 @@ class DensityMatrix(StateVector):
         if ref.ndim == 2:
             ref = ref.T.ravel()
         return super().agreesWith(ref, tol)
+
+
+def load(path):
+    """The StateVector or DensityMatrix stored in a state file (``dfs_state_load``)."""
+    h = C.c_void_p()
+    call("dfs_state_load", os.fsencode(path), C.byref(h))
+    info = StateInfo()
+    call("dfs_state_get_info", h, C.byref(info))
+    cls = DensityMatrix if info.is_density_matrix else StateVector
+    return cls(info.num_qubits, _handle=h)
 
 
 def _dm_check(rho) -> None:

@@ -212,6 +212,7 @@ const char* dfs_error_string(int code) {
         case DFS_ERR_NOT_INITIALISED: return "not initialised";
         case DFS_ERR_PRECISION: return "precision mismatch";
         case DFS_ERR_TIMEOUT: return "device wait timed out";
+        case DFS_ERR_IO: return "state file error";
         default: return "unknown error";
     }
 }

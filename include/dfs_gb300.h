@@ -50,7 +50,8 @@ enum {
     DFS_ERR_CUDA = 7,            /* a CUDA runtime call failed */
     DFS_ERR_NOT_INITIALISED = 8, /* dfs_comm_init() has not been called */
     DFS_ERR_PRECISION = 9,       /* states of different precisions combined */
-    DFS_ERR_TIMEOUT = 10         /* a bounded device-side wait gave up */
+    DFS_ERR_TIMEOUT = 10,        /* a bounded device-side wait gave up */
+    DFS_ERR_IO = 11              /* a state file could not be opened, read, written or parsed */
 };
 
 const char* dfs_error_string(int code);
@@ -124,6 +125,21 @@ int dfs_state_set_classical(dfs_state s, uint64_t index);
  * the same seed gives the same state on any GPU), optionally normalised to
  * unit 2-norm.  Replaces setRandomAmps, tests/test_utilities.hpp:438-448. */
 int dfs_state_set_random(dfs_state s, uint64_t seed, int normalise);
+
+/* ---------------------------------------------------------- state files */
+/* Checkpoint and interchange file of one state (no reference counterpart; its
+ * amplitude order is getAllVecAmps', tests/test_utilities.hpp:419-435, and a density
+ * matrix's element (r, c) sits at r + c 2^n as in getAllMatrAmps,
+ * tests/test_utilities.hpp:490-503).  Little-endian, a 40-byte header then the data:
+ *   char[8] "DFSSTATE" | u32 version = 1 | u32 kind (0 statevector, 1 density matrix) |
+ *   u32 num_qubits (of the matrix, for a density matrix) | i32 precision (DFS_C128 ...) |
+ *   u64 num_amps | u32 bytes per amplitude (16 complex128, 8 complex64) | u32 0
+ * followed by num_amps interleaved (re, im) pairs in the state's storage format.
+ * Amplitudes stream through pinned host memory in chunks, so a state needs no
+ * host buffer of its own size. */
+int dfs_state_save(dfs_state s, const char* path);
+/* a new state of the file's kind, size and precision holding its amplitudes */
+int dfs_state_load(const char* path, dfs_state* out);
 
 /* ------------------------------------------------------ statevector gates */
 /* All act on statevectors and, through the 2n-qubit view, on any state. */
