@@ -81,6 +81,9 @@ PROTOTYPES = {
     "dfs_state_get_amps": [_H, _DP, _U64, _U64],
     "dfs_state_set_raw": [_H, _V, _U64, _U64],
     "dfs_state_get_raw": [_H, _V, _U64, _U64],
+    "dfs_state_set_raw_async": [_H, _V, _U64, _U64],
+    "dfs_state_get_raw_async": [_H, _V, _U64, _U64],
+    "dfs_state_wait_transfers": [_H],
     "dfs_state_copy": [_H, _H],
     "dfs_state_set_zero": [_H],
     "dfs_state_set_classical": [_H, _U64],

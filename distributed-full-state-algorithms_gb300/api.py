@@ -161,6 +161,30 @@ class StateVector:
         call("dfs_state_device_ptr", self._h, C.byref(p))
         return p.value or 0
 
+    # ---- asynchronous transfers (the state's storage format; page-locked host memory) ----
+    @staticmethod
+    def _host_ptr(buf) -> int:
+        return int(buf.data_ptr()) if hasattr(buf, "data_ptr") else int(buf.ctypes.data)
+
+    def _raw_count(self, buf) -> int:
+        nbytes = int(buf.numel() * buf.element_size()) if hasattr(buf, "numel") else int(buf.nbytes)
+        return nbytes // (8 if self.precision == "c64" else 16)
+
+    def uploadAsync(self, buf, start: int = 0) -> None:
+        """Copy ``buf`` (raw amplitudes: complex128, or complex64 for a "c64" state)
+        into the state from ``start`` on the engine's copy stream, overlapping other
+        work; later operations on the state wait for it.  ``buf`` must stay alive and
+        untouched until ``waitTransfers``."""
+        call("dfs_state_set_raw_async", self._h, C.c_void_p(self._host_ptr(buf)), int(start), self._raw_count(buf))
+
+    def downloadAsync(self, buf, start: int = 0) -> None:
+        """Copy amplitudes from ``start`` into ``buf`` after every operation issued on
+        the state so far, on the copy stream; ``waitTransfers`` makes ``buf`` valid."""
+        call("dfs_state_get_raw_async", self._h, C.c_void_p(self._host_ptr(buf)), int(start), self._raw_count(buf))
+
+    def waitTransfers(self) -> None:
+        call("dfs_state_wait_transfers", self._h)
+
     def save(self, path) -> None:
         """Write the state to a file (``dfs_state_save``; the layout is in
         ``state_file.py``)."""

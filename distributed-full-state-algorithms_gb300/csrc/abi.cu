@@ -110,9 +110,18 @@ int upload_scratch(const void* host, size_t bytes, size_t offset) {
 
 // ----------------------------------------------------------- validation
 
+int state_acquire(State* s) {
+    if (!s->copyPending) return DFS_SUCCESS;
+    cudaError_t e = cudaStreamWaitEvent(g_ctx.stream, s->copyDone, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "wait for a state transfer");
+    s->copyPending = false;
+    return DFS_SUCCESS;
+}
+
 static int check_state(dfs_state s) {
     if (!s) return fail(DFS_ERR_INVALID_ARG, "null state handle");
-    return ensure_init();
+    int rc = ensure_init();
+    return rc ? rc : state_acquire(s);
 }
 
 static int check_dm(dfs_state s) {
@@ -272,6 +281,10 @@ int dfs_densitymatrix_create(unsigned n, int precision, dfs_state* out) { return
 int dfs_state_destroy(dfs_state s) {
     if (!s) return DFS_SUCCESS;
     if (g_ctx.initialised) cudaStreamSynchronize(g_ctx.stream);
+    if (s->copyDone) {
+        cudaEventSynchronize(s->copyDone);
+        cudaEventDestroy(s->copyDone);
+    }
     cudaFree(s->amps);
     delete s;
     return DFS_SUCCESS;
@@ -292,12 +305,18 @@ int dfs_state_get_info(dfs_state s, dfs_state_info* info) {
 
 int dfs_state_device_ptr(dfs_state s, void** ptr) {
     if (!s || !ptr) return fail(DFS_ERR_INVALID_ARG, "null argument");
+    // the caller may use the buffer on any stream: finish pending transfers first
+    if (s->copyPending) {
+        cudaError_t e = cudaEventSynchronize(s->copyDone);
+        if (e != cudaSuccess) return cuda_fail(e, "wait for a state transfer");
+        s->copyPending = false;
+    }
     *ptr = s->amps;
     return DFS_SUCCESS;
 }
 
-static int check_range(dfs_state s, const void* p, uint64_t start, uint64_t count) {
-    int rc = check_state(s);
+static int check_range(dfs_state s, const void* p, uint64_t start, uint64_t count, bool acquire = true) {
+    int rc = acquire ? check_state(s) : (s ? ensure_init() : fail(DFS_ERR_INVALID_ARG, "null state handle"));
     if (rc) return rc;
     if (count && !p) return fail(DFS_ERR_INVALID_ARG, "null buffer");
     if (start > s->numAmps || count > s->numAmps - start)
@@ -334,6 +353,46 @@ int dfs_state_get_raw(dfs_state s, void* dst, uint64_t start, uint64_t count) {
         cudaMemcpyAsync(dst, (const char*)s->amps + start * eb, count * eb, cudaMemcpyDeviceToHost, g_ctx.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g_ctx.stream);
     return e == cudaSuccess ? DFS_SUCCESS : cuda_fail(e, "get_raw");
+}
+
+// asynchronous raw transfer on the copy stream, after the work already queued on the
+// compute stream (which covers every earlier operation on the state) and, in stream
+// order, after the state's earlier transfers
+static int transfer_async(dfs_state s, void* host, uint64_t start, uint64_t count, bool toDevice) {
+    // no state_acquire: the copy stream orders this after the state's earlier transfers,
+    // and the compute stream must not wait for them here
+    int rc = check_range(s, host, start, count, false);
+    if (rc || !count) return rc;
+    cudaError_t e = cudaSuccess;
+    if (!g_ctx.copyStream) e = cudaStreamCreateWithFlags(&g_ctx.copyStream, cudaStreamNonBlocking);
+    if (e == cudaSuccess && !g_ctx.computeMark) e = cudaEventCreateWithFlags(&g_ctx.computeMark, cudaEventDisableTiming);
+    if (e == cudaSuccess && !s->copyDone) e = cudaEventCreateWithFlags(&s->copyDone, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(g_ctx.computeMark, g_ctx.stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(g_ctx.copyStream, g_ctx.computeMark, 0);
+    const size_t eb = elem_bytes(s->precision);
+    char* dev = (char*)s->amps + start * eb;
+    if (e == cudaSuccess)
+        e = toDevice ? cudaMemcpyAsync(dev, host, count * eb, cudaMemcpyHostToDevice, g_ctx.copyStream)
+                     : cudaMemcpyAsync(host, dev, count * eb, cudaMemcpyDeviceToHost, g_ctx.copyStream);
+    if (e == cudaSuccess) e = cudaEventRecord(s->copyDone, g_ctx.copyStream);
+    if (e != cudaSuccess) return cuda_fail(e, "asynchronous state transfer");
+    s->copyPending = true;
+    return DFS_SUCCESS;
+}
+
+int dfs_state_set_raw_async(dfs_state s, const void* src, uint64_t start, uint64_t count) {
+    return transfer_async(s, const_cast<void*>(src), start, count, true);
+}
+
+int dfs_state_get_raw_async(dfs_state s, void* dst, uint64_t start, uint64_t count) {
+    return transfer_async(s, dst, start, count, false);
+}
+
+int dfs_state_wait_transfers(dfs_state s) {
+    if (!s) return fail(DFS_ERR_INVALID_ARG, "null state handle");
+    if (!s->copyDone) return DFS_SUCCESS;
+    cudaError_t e = cudaEventSynchronize(s->copyDone);
+    return e == cudaSuccess ? DFS_SUCCESS : cuda_fail(e, "wait for a state transfer");
 }
 
 int dfs_state_copy(dfs_state dst, dfs_state src) {

@@ -507,6 +507,8 @@ int dfs_batch_set_state(dfs_batch b, unsigned index, dfs_state s) {
     if (index >= b->num) return fail(DFS_ERR_INVALID_ARG, "circuit %u of %u", index, b->num);
     if (s->isDM || s->numQubits != b->nq[index]) return fail(DFS_ERR_STATE_KIND, "state does not match circuit %u", index);
     if (s->precision != b->precision) return fail(DFS_ERR_PRECISION, "state precision differs from the batch's");
+    int rc = state_acquire(s);
+    if (rc) return rc;
     State v = arena_view(b, 0, index);
     cudaError_t e = cudaMemcpyAsync(v.amps, s->amps, v.numAmps * elem_bytes(b->precision), cudaMemcpyDeviceToDevice,
                                     ctx().stream);
@@ -530,6 +532,8 @@ int dfs_batch_get_state(dfs_batch b, unsigned index, dfs_state out) {
     if (index >= b->num) return fail(DFS_ERR_INVALID_ARG, "circuit %u of %u", index, b->num);
     if (out->isDM || out->numQubits != b->nq[index] || out->precision != b->precision)
         return fail(DFS_ERR_STATE_KIND, "state does not match circuit %u", index);
+    int rc = state_acquire(out);
+    if (rc) return rc;
     State v = arena_view(b, 1, index);
     cudaError_t e = cudaMemcpyAsync(out->amps, v.amps, v.numAmps * elem_bytes(b->precision),
                                     cudaMemcpyDeviceToDevice, ctx().stream);

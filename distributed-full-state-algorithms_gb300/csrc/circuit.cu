@@ -700,13 +700,13 @@ static int check_circuit(const Circuit* c) {
     return c ? DFS_SUCCESS : fail(DFS_ERR_INVALID_ARG, "null circuit");
 }
 
-static int check_state_for(const Circuit* c, const State* s) {
+static int check_state_for(const Circuit* c, State* s) {
     if (!s) return fail(DFS_ERR_INVALID_ARG, "null state");
     if (s->isDM != c->isDM || s->numQubits != c->numQubits)
         return fail(DFS_ERR_STATE_KIND, "state (%s, %u qubits) does not match the circuit (%s, %u qubits)",
                     s->isDM ? "density matrix" : "statevector", s->numQubits,
                     c->isDM ? "density matrix" : "statevector", c->numQubits);
-    return DFS_SUCCESS;
+    return state_acquire(s);
 }
 
 static int check_params(const Circuit* c, const double* params) {

@@ -28,6 +28,9 @@ struct Context {
     cudaEvent_t pinnedFree = nullptr;
     // dense gates on 3-4 targets go to the tensor cores (DFS_DENSE_TC=0 disables)
     bool denseTensorCores = true;
+    // asynchronous host transfers (dfs_state_*_raw_async) run here, beside `stream`
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t computeMark = nullptr;
 };
 
 Context& ctx();
@@ -39,7 +42,14 @@ struct State {
     uint64_t numAmps;     // 2^vecQubits
     int precision;
     void* amps;
+    // the latest asynchronous transfer of this state, recorded on the copy stream; work
+    // on the compute stream waits for it once (state_acquire)
+    cudaEvent_t copyDone = nullptr;
+    bool copyPending = false;
 };
+
+// orders the context stream after the state's pending asynchronous transfer
+int state_acquire(State* s);
 
 // records a message for dfs_last_error and returns code
 int fail(int code, const char* fmt, ...);

@@ -178,5 +178,7 @@ extern "C" int dfs_densitymatrix_expecPauliString_noalloc(dfs_state s, const dou
         *im = 0;
         return DFS_SUCCESS;
     }
+    int rc = state_acquire(s);
+    if (rc) return rc;
     return dispatch<RunExpecDMNoAlloc>(s, s, coeffs, numTerms, allPaulis, re, im);
 }

@@ -113,6 +113,15 @@ int dfs_state_get_amps(dfs_state s, double* amps, uint64_t start, uint64_t count
 /* same, from/to host memory in the state's own device format (no conversion) */
 int dfs_state_set_raw(dfs_state s, const void* src, uint64_t start, uint64_t count);
 int dfs_state_get_raw(dfs_state s, void* dst, uint64_t start, uint64_t count);
+/* Asynchronous forms of set_raw / get_raw: the copy runs on the engine's copy stream,
+ * overlapping gates on other states, ordered after every operation already issued on
+ * this state; every later operation on the state waits for it.  Host memory should be
+ * page-locked (otherwise the copy is staged synchronously) and must stay untouched
+ * until dfs_state_wait_transfers(s) returns.  No reference counterpart. */
+int dfs_state_set_raw_async(dfs_state s, const void* src, uint64_t start, uint64_t count);
+int dfs_state_get_raw_async(dfs_state s, void* dst, uint64_t start, uint64_t count);
+/* block the host until the state's asynchronous transfers have completed */
+int dfs_state_wait_transfers(dfs_state s);
 /* device-to-device copy between two states of equal shape; between complex64 and
  * complex128 storage the amplitudes are converted (exact widening, round-to-nearest
  * narrowing) */

@@ -99,3 +99,71 @@ def test_engine_refuses_bad_files(dfs, tmp_path):
     assert e.value.code == 11
     with pytest.raises(dfs.DfsError):
         dfs.load(tmp_path / "missing.dfs")
+
+
+# ---- asynchronous transfers (dfs_state_*_raw_async) ----
+
+def _pinned(n, dtype):
+    torch = pytest.importorskip("torch")
+    t = torch.empty(n, dtype=torch.complex128 if dtype == np.complex128 else torch.complex64, pin_memory=True)
+    return t, t.numpy()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+def test_async_transfers_order_with_gates(dfs, oracle, rng, prec):
+    n = 16
+    dt = np.complex64 if prec == "c64" else np.complex128
+    a = gaussian_state(rng, 1 << n).astype(dt)
+    tin, hin = _pinned(1 << n, dt)
+    tout, hout = _pinned(1 << n, dt)
+    tmid, hmid = _pinned(1 << n, dt)
+    hin[:] = a
+    psi = dfs.StateVector(n, precision=prec)
+    u = np.array([[0.6, 0.8j], [0.8j, 0.6]])
+    psi.uploadAsync(tin)                            # the gate below must see these amplitudes
+    dfs.distributed_statevector_oneTargGate(psi, 3, u)
+    psi.downloadAsync(tmid)                         # after the first gate ...
+    dfs.distributed_statevector_oneTargGate(psi, 9, u)  # ... not after this one
+    psi.downloadAsync(tout)
+    psi.waitTransfers()
+    ref = a.astype(np.complex128)
+    oracle.sv_one_targ(ref, 3, u)
+    tol = 1e-6 if prec == "c64" else 1e-12
+    assert np.max(np.abs(hmid - ref)) <= tol
+    oracle.sv_one_targ(ref, 9, u)
+    assert np.max(np.abs(hout - ref)) <= tol
+    assert np.array_equal(hout, psi.getAllVecAmps().astype(dt))
+
+
+@pytest.mark.gpu
+def test_async_pipeline_two_states(dfs, oracle, rng):
+    """The serving loop of the end-to-end benchmark: state i+1 uploads and state i-1
+    downloads while state i runs its gates."""
+    n, steps = 14, 5
+    bufs = [_pinned(1 << n, np.complex128) for _ in range(2)]
+    inputs = [gaussian_state(rng, 1 << n) for _ in range(steps)]
+    states = [dfs.StateVector(n), dfs.StateVector(n)]
+    g = np.array([[0.6, 0.8], [-0.8, 0.6]], dtype=np.complex128)
+    outputs = []
+    bufs[0][1][:] = inputs[0]
+    states[0].uploadAsync(bufs[0][0])
+    for i in range(steps):
+        cur, nxt = states[i % 2], states[(i + 1) % 2]
+        if i + 1 < steps:
+            if i >= 1:
+                nxt.waitTransfers()                 # its download of step i-1 has landed
+                outputs.append(bufs[(i + 1) % 2][1].copy())
+            bufs[(i + 1) % 2][1][:] = inputs[i + 1]
+            nxt.uploadAsync(bufs[(i + 1) % 2][0])
+        for q in range(n):
+            dfs.distributed_statevector_oneTargGate(cur, q, g)
+        cur.downloadAsync(bufs[i % 2][0])
+    for j in (steps - 2, steps - 1):
+        states[j % 2].waitTransfers()
+        outputs.append(bufs[j % 2][1].copy())
+    for i in range(steps):
+        ref = inputs[i].copy()
+        for q in range(n):
+            oracle.sv_one_targ(ref, q, g)
+        assert np.max(np.abs(outputs[i] - ref)) <= 1e-12
