@@ -170,22 +170,6 @@ DEV typename P::V rot(typename P::V x, int k, int s) {
     return r;
 }
 
-// ----------------------------------------------------------- reductions
-// Partial sums of every policy accumulate in double-float (FP64 class):
-// GB300's FP64 adder runs at ~1.9 ops/clk/SM, too slow to sit in a stream.
-struct DSum {
-    df::f2 v;
-};
-DEV df::f2 dsum_add(df::f2 a, float x) {
-    df::f2 t = df::two_sum(a.hi, x);
-    return df::fast_two_sum(t.hi, df::add_rn(t.lo, a.lo));
-}
-DEV df::f2 dsum_add2(df::f2 a, df::f2 b) {
-    df::f2 t = df::two_sum(a.hi, b.hi);
-    return df::fast_two_sum(t.hi, df::add_rn(t.lo, df::add_rn(a.lo, b.lo)));
-}
-DEV double dsum_to_double(df::f2 a) { return (double)a.hi + (double)a.lo; }
-
 // ------------------------------------------------------------- launches
 
 struct Launch {

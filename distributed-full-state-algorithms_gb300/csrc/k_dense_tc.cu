@@ -89,15 +89,6 @@ DEV uint64_t fraction48(uint32_t H, uint32_t L, uint32_t E) {
     return ex == 0u ? 0ull : F;
 }
 
-// sign * b for byte `sel` (0..3) of `word`, as an exact float: the byte is
-// placed under the exponent of the magic +-2^23 (one PRMT), then the magic is
-// subtracted; the float's top 16 bits are the bf16 of the same value
-template <int SEL>
-DEV float float_of_byte(uint32_t word, uint32_t magicBits, float magic) {
-    // result bytes: [magic.b3, magic.b2 (0), magic.b1 (0), word.bSEL]
-    const uint32_t f = __byte_perm(word, magicBits, 0x7650u | SEL);
-    return __fsub_rn(__uint_as_float(f), magic);
-}
 // the bf16 halves of two floats packed as (lo, hi)
 DEV uint32_t pack_bf16(float lo, float hi) { return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632u); }
 

@@ -40,8 +40,6 @@ DEV df::f2 dfprod(float a, float b) {
     float p = df::mul_rn(a, b);
     return {p, df::fmaf_(a, b, -p)};
 }
-// a * b for df values (dropping lo*lo)
-DEV df::f2 dfmul(df::f2 a, df::f2 b) { return df::acc_result(df::acc_first(a, b)); }
 
 DEV void sum_zero(SumDF& s) { s.re = {0.f, 0.f}; s.im = {0.f, 0.f}; }
 DEV void sum_zero(SumF64& s) { s.re = 0.0; s.im = 0.0; }
