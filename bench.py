@@ -159,6 +159,17 @@ def replica_throughput(local_ms: float, units_per_rank: int, world: int, device=
     return world * units_per_rank / (ms / 1e3), ms
 
 
+def any_rank(flag: bool, world: int) -> bool:
+    """Whether `flag` holds on any rank (so that every rank takes the same branch)."""
+    if world == 1:
+        return flag
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([1.0 if flag else 0.0], dtype=torch.float64, device="cuda")
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item()) > 0
+
+
 def roofline_traffic(kind: str):
     """dram read+write bytes per launch of `kind` from the committed ncu summary."""
     f = ROOT / "profiles" / "ncu_sv30_gate_mix.md"
@@ -375,7 +386,14 @@ def gpu_arm(args, world, rank, local):
     if not args.no_extras:
         import ctypes as C
         lib = dfs.load_library()
-        hosts = [torch.empty(num_amps * 2, dtype=torch.float64, pin_memory=True) for _ in range(2)]
+        hosts = [torch.empty(num_amps * 2, dtype=torch.float64, pin_memory=True)]
+        psi2 = None
+        try:  # the serving loop's second pinned buffer and device state
+            hosts.append(torch.empty(num_amps * 2, dtype=torch.float64, pin_memory=True))
+            psi2 = dfs.StateVector(n)
+        except (RuntimeError, dfs.DfsError):
+            pass
+        serving = not any_rank(psi2 is None, world)
         for h in hosts:  # valid input states
             assert lib.dfs_state_get_raw(psi.handle, C.c_void_p(h.data_ptr()), 0, num_amps) == 0
         e2e_steps = max(2, min(4, args.steps))
@@ -390,34 +408,38 @@ def gpu_arm(args, world, rank, local):
             assert lib.dfs_state_get_raw(psi.handle, ptr, 0, num_amps) == 0
         barrier()
         blocking_s = time.perf_counter() - t0
-        # the same as a serving loop: the transfers go on the engine's copy stream
-        # (dfs_state_set_raw_async / get_raw_async), so step i+1's upload and step i-1's
-        # download overlap step i's gates; two device states, two pinned buffers (step
-        # i + 2 takes step i's output as its input)
-        psi2 = dfs.StateVector(n)
-        states = [psi, psi2]
-        barrier()
-        t0 = time.perf_counter()
-        states[0].uploadAsync(hosts[0])
-        for i in range(e2e_steps):
-            cur, nxt = states[i % 2], states[(i + 1) % 2]
-            if i + 1 < e2e_steps:
-                nxt.uploadAsync(hosts[(i + 1) % 2])
-            circuits.apply(dfs, cur, gates)
-            cur.downloadAsync(hosts[i % 2])
-        for st in states:
-            st.waitTransfers()
-        dfs.comm_synch()
-        barrier()
-        e2e_s = time.perf_counter() - t0
         per_step = {"h2d_bytes_per_step": num_amps * elem, "d2h_bytes_per_step": num_amps * elem}
-        result["e2e"] = {"value": world * len(gates) * e2e_steps / e2e_s, "unit": "gates/s", **per_step,
-                         "mode": f"serving loop of {e2e_steps} steps, transfers overlapped on a copy stream"}
-        result["e2e_blocking"] = {"value": world * len(gates) * e2e_steps / blocking_s, "unit": "gates/s",
-                                  **per_step, "mode": "upload, circuit, download in turn"}
+        blocking = {"value": world * len(gates) * e2e_steps / blocking_s, "unit": "gates/s", **per_step,
+                    "mode": "upload, circuit, download in turn"}
+        if serving:
+            # the same as a serving loop: the transfers go on the engine's copy stream
+            # (dfs_state_set_raw_async / get_raw_async), so step i+1's upload and step i-1's
+            # download overlap step i's gates; two device states, two pinned buffers (step
+            # i + 2 takes step i's output as its input)
+            states = [psi, psi2]
+            barrier()
+            t0 = time.perf_counter()
+            states[0].uploadAsync(hosts[0])
+            for i in range(e2e_steps):
+                cur, nxt = states[i % 2], states[(i + 1) % 2]
+                if i + 1 < e2e_steps:
+                    nxt.uploadAsync(hosts[(i + 1) % 2])
+                circuits.apply(dfs, cur, gates)
+                cur.downloadAsync(hosts[i % 2])
+            for st in states:
+                st.waitTransfers()
+            dfs.comm_synch()
+            barrier()
+            e2e_s = time.perf_counter() - t0
+            result["e2e"] = {"value": world * len(gates) * e2e_steps / e2e_s, "unit": "gates/s", **per_step,
+                             "mode": f"serving loop of {e2e_steps} steps, transfers overlapped on a copy stream"}
+            result["e2e_blocking"] = blocking
+        else:  # no room for a second state or pinned buffer on some rank
+            result["e2e"] = blocking
         del hosts
         psi.free()
-        psi2.free()
+        if psi2 is not None:
+            psi2.free()
 
         # FP32 form: the same circuit on a complex64 state
         phi = dfs.StateVector(n, precision="c64")
