@@ -396,7 +396,7 @@ def gpu_arm(args, world, rank, local):
         serving = not any_rank(psi2 is None, world)
         for h in hosts:  # valid input states
             assert lib.dfs_state_get_raw(psi.handle, C.c_void_p(h.data_ptr()), 0, num_amps) == 0
-        e2e_steps = max(2, min(4, args.steps))
+        e2e_steps = max(2, min(6, args.steps + 2))  # the serving loop amortises its first upload and last download
         # end to end through the public API with host buffers, as a blocking loop: upload
         # the step's input state from pinned memory, run the circuit, read it back
         ptr = C.c_void_p(hosts[0].data_ptr())
