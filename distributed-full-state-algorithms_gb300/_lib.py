@@ -88,6 +88,7 @@ PROTOTYPES = {
     "dfs_state_set_zero": [_H],
     "dfs_state_set_classical": [_H, _U64],
     "dfs_state_set_random": [_H, _U64, _I],
+    "dfs_wait_selftest": [_D, _U, C.POINTER(_I), C.POINTER(_I)],
     "dfs_state_save": [_H, C.c_char_p],
     "dfs_state_load": [C.c_char_p, _HP],
     "dfs_statevector_oneTargGate": [_H, _U, _DP],

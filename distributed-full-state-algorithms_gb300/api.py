@@ -24,7 +24,7 @@ from ._lib import DfsError, StateInfo, call
 
 __all__ = [
     "DfsError", "StateVector", "DensityMatrix", "comm_init", "comm_end", "comm_getRank", "comm_getNumNodes",
-    "comm_synch", "set_stream", "load",
+    "comm_synch", "set_stream", "load", "wait_selftest",
     "distributed_statevector_oneTargGate", "distributed_statevector_manyCtrlOneTargGate",
     "distributed_statevector_swapGate", "distributed_statevector_manyTargGate",
     "distributed_statevector_pauliTensor", "distributed_statevector_pauliGadget",
@@ -223,6 +223,15 @@ class DensityMatrix(StateVector):
         if ref.ndim == 2:
             ref = ref.T.ravel()
         return super().agreesWith(ref, tol)
+
+
+def wait_selftest(seconds: float = 0.05, polls: int = 4096) -> tuple[bool, bool]:
+    """Run the device-side failure-detection self-test (``dfs_wait_selftest``): a spin on
+    a word nothing writes and an mbarrier phase that never completes, each given up after
+    its limit.  Returns (spin gave up, mbarrier wait gave up)."""
+    a, b = C.c_int(), C.c_int()
+    call("dfs_wait_selftest", float(seconds), int(polls), C.byref(a), C.byref(b))
+    return bool(a.value), bool(b.value)
 
 
 def load(path):

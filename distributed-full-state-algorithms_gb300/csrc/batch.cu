@@ -677,4 +677,12 @@ int dfs_batch_autotune(dfs_batch b, int withGradient, double* best_ms) {
     return DFS_SUCCESS;
 }
 
+int dfs_wait_selftest(double seconds, unsigned polls, int* spinTimedOut, int* mbarTimedOut) {
+    if (!spinTimedOut || !mbarTimedOut) return fail(DFS_ERR_INVALID_ARG, "null output");
+    if (!(seconds > 0 && seconds <= 10) || polls == 0)
+        return fail(DFS_ERR_INVALID_ARG, "limits must be in (0, 10] seconds and > 0 polls");
+    if (!ctx().initialised) return fail(DFS_ERR_NOT_INITIALISED, "dfs_comm_init() has not been called");
+    return batch::wait_selftest(seconds, polls, spinTimedOut, mbarTimedOut);
+}
+
 }  // extern "C"

@@ -68,6 +68,8 @@ struct Args {
 int launch(int precision, const Args& a, unsigned grid, cudaStream_t stream);
 // largest co-resident CTAs per SM of the kernel
 int max_ctas_per_sm(int precision, int* out);
+// runs the bounded-wait self-test kernel (see dfs_wait_selftest)
+int wait_selftest(double seconds, uint32_t polls, int* spinTimedOut, int* mbarTimedOut);
 
 }  // namespace batch
 }  // namespace dfs

@@ -14,6 +14,7 @@
 
 #include "batch.hpp"
 #include "kernels.cuh"
+#include "tc.cuh"
 #include "reduce.cuh"
 #include "tile_ops.cuh"
 
@@ -34,6 +35,21 @@ DEV unsigned ld_acquire(const unsigned* p) {
     return v;
 }
 
+// the bounded spin of every cross-CTA wait: until *word != seen; false when another
+// waiter raised *err or `limitNs` passed (then this one raises it)
+DEV bool spin_while_equal(const unsigned* word, unsigned seen, int* err, uint64_t limitNs) {
+    const uint64_t t0 = global_ns();
+    while (ld_acquire(word) == seen) {
+        if (*(volatile int*)err) return false;
+        if (global_ns() - t0 > limitNs) {
+            atomicExch(err, 1);
+            return false;
+        }
+        __nanosleep(64);
+    }
+    return true;
+}
+
 // team barrier: false when this CTA (or another) gave up waiting
 DEV bool team_sync(const Args& a, TeamSync* ts, unsigned& gen) {
     __shared__ int ok;
@@ -47,26 +63,47 @@ DEV bool team_sync(const Args& a, TeamSync* ts, unsigned& gen) {
             atomicExch(&ts->count, 0u);
             __threadfence();
             atomicAdd(&ts->gen, 1u);
-        } else {
-            const uint64_t t0 = global_ns();
-            while (ld_acquire(&ts->gen) == gen) {
-                if (*(volatile int*)a.err) {
-                    ok = 0;
-                    break;
-                }
-                if (global_ns() - t0 > kWaitNs) {
-                    atomicExch(a.err, 1);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
-            }
+        } else if (!spin_while_equal(&ts->gen, gen, a.err, kWaitNs)) {
+            ok = 0;
         }
         gen++;
         __threadfence();
     }
     __syncthreads();
     return ok != 0;
+}
+
+// Self-test of the bounded waits on waits that cannot complete: status[0] = 1 when the
+// spin on a word nothing writes gave up after `limitNs`; status[1] = 1 when an mbarrier
+// wait for a phase that never completes (one arrival of two) gave up after its poll
+// limit.  Nothing faults or hangs: both waits end and the kernel returns.
+__global__ void k_wait_selftest(const unsigned* word, int* status, uint64_t limitNs, uint32_t polls) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x != 0) return;
+    status[0] = spin_while_equal(word, 0u, status + 2, limitNs) ? 0 : (*(volatile int*)(status + 2) ? 1 : 0);
+    tc::mbar_init(&bar, 2);
+    tc::mbar_arrive(&bar);
+    status[1] = tc::mbar_wait(&bar, 0, polls) ? 0 : 1;
+}
+
+int wait_selftest(double seconds, uint32_t polls, int* spinTimedOut, int* mbarTimedOut) {
+    void* mem = nullptr;
+    cudaError_t e = cudaMalloc(&mem, 16);
+    if (e != cudaSuccess) return cuda_fail(e, "self-test buffer");
+    int h[3] = {0, 0, 0};
+    e = cudaMemsetAsync(mem, 0, 16, ctx().stream);
+    if (e == cudaSuccess) {
+        k_wait_selftest<<<1, 32, 0, ctx().stream>>>((const unsigned*)mem, (int*)((char*)mem + 4),
+                                                    (uint64_t)(seconds * 1e9), polls);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, (char*)mem + 4, sizeof h, cudaMemcpyDeviceToHost, ctx().stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx().stream);
+    cudaFree(mem);
+    if (e != cudaSuccess) return cuda_fail(e, "wait self-test");
+    *spinTimedOut = h[0];
+    *mbarTimedOut = h[1];
+    return DFS_SUCCESS;
 }
 
 // ------------------------------------------------------------ one circuit

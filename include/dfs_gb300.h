@@ -135,6 +135,14 @@ int dfs_state_set_classical(dfs_state s, uint64_t index);
  * unit 2-norm.  Replaces setRandomAmps, tests/test_utilities.hpp:438-448. */
 int dfs_state_set_random(dfs_state s, uint64_t seed, int normalise);
 
+/* Self-test of the device-side failure detection (no reference counterpart): one
+ * kernel spins, as the batched kernel's team barrier does, on a word nothing writes
+ * until `seconds` have passed by the global timer, and waits, as the tensor-core
+ * kernels do, on an mbarrier phase that never completes until `polls` polls; both
+ * waits give up and report it (*spin_timed_out, *mbar_timed_out = 1) and the kernel
+ * returns, so the context stays usable.  Nothing faults or hangs. */
+int dfs_wait_selftest(double seconds, unsigned polls, int* spin_timed_out, int* mbar_timed_out);
+
 /* ---------------------------------------------------------- state files */
 /* Checkpoint and interchange file of one state (no reference counterpart; its
  * amplitude order is getAllVecAmps', tests/test_utilities.hpp:419-435, and a density
