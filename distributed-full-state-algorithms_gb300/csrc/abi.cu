@@ -233,6 +233,7 @@ const char* dfs_last_error(void) { return g_lastError; }
 int dfs_comm_init(void) { return ensure_init(); }
 
 int dfs_comm_end(void) {
+    DFS_TRACE_CALL();
     if (!g_ctx.initialised) return DFS_SUCCESS;
     cudaStreamSynchronize(g_ctx.stream);
     return DFS_SUCCESS;
@@ -251,6 +252,7 @@ int dfs_comm_get_num_nodes(unsigned* n) {
 }
 
 int dfs_comm_synch(void) {
+    DFS_TRACE_CALL();
     int rc = ensure_init();
     if (rc) return rc;
     cudaError_t e = cudaStreamSynchronize(g_ctx.stream);
@@ -279,6 +281,7 @@ int dfs_statevector_create(unsigned n, int precision, dfs_state* out) { return n
 int dfs_densitymatrix_create(unsigned n, int precision, dfs_state* out) { return new_state(n, 1, precision, out); }
 
 int dfs_state_destroy(dfs_state s) {
+    DFS_TRACE_CALL();
     if (!s) return DFS_SUCCESS;
     if (g_ctx.initialised) cudaStreamSynchronize(g_ctx.stream);
     if (s->copyDone) {
@@ -326,16 +329,19 @@ static int check_range(dfs_state s, const void* p, uint64_t start, uint64_t coun
 }
 
 int dfs_state_set_amps(dfs_state s, const double* amps, uint64_t start, uint64_t count) {
+    DFS_TRACE_CALL();
     int rc = check_range(s, amps, start, count);
     return rc ? rc : (count ? state_upload(s, amps, start, count) : DFS_SUCCESS);
 }
 
 int dfs_state_get_amps(dfs_state s, double* amps, uint64_t start, uint64_t count) {
+    DFS_TRACE_CALL();
     int rc = check_range(s, amps, start, count);
     return rc ? rc : (count ? state_download(s, amps, start, count) : DFS_SUCCESS);
 }
 
 int dfs_state_set_raw(dfs_state s, const void* src, uint64_t start, uint64_t count) {
+    DFS_TRACE_CALL();
     int rc = check_range(s, src, start, count);
     if (rc || !count) return rc;
     size_t eb = elem_bytes(s->precision);
@@ -346,6 +352,7 @@ int dfs_state_set_raw(dfs_state s, const void* src, uint64_t start, uint64_t cou
 }
 
 int dfs_state_get_raw(dfs_state s, void* dst, uint64_t start, uint64_t count) {
+    DFS_TRACE_CALL();
     int rc = check_range(s, dst, start, count);
     if (rc || !count) return rc;
     size_t eb = elem_bytes(s->precision);
@@ -381,14 +388,17 @@ static int transfer_async(dfs_state s, void* host, uint64_t start, uint64_t coun
 }
 
 int dfs_state_set_raw_async(dfs_state s, const void* src, uint64_t start, uint64_t count) {
+    DFS_TRACE_CALL();
     return transfer_async(s, const_cast<void*>(src), start, count, true);
 }
 
 int dfs_state_get_raw_async(dfs_state s, void* dst, uint64_t start, uint64_t count) {
+    DFS_TRACE_CALL();
     return transfer_async(s, dst, start, count, false);
 }
 
 int dfs_state_wait_transfers(dfs_state s) {
+    DFS_TRACE_CALL();
     if (!s) return fail(DFS_ERR_INVALID_ARG, "null state handle");
     if (!s->copyDone) return DFS_SUCCESS;
     cudaError_t e = cudaEventSynchronize(s->copyDone);
@@ -396,6 +406,7 @@ int dfs_state_wait_transfers(dfs_state s) {
 }
 
 int dfs_state_copy(dfs_state dst, dfs_state src) {
+    DFS_TRACE_CALL();
     int rc = check_state(dst);
     if (!rc) rc = check_state(src);
     if (rc) return rc;
@@ -409,11 +420,13 @@ int dfs_state_copy(dfs_state dst, dfs_state src) {
 }
 
 int dfs_state_set_zero(dfs_state s) {
+    DFS_TRACE_CALL();
     int rc = check_state(s);
     return rc ? rc : state_fill_zero(s);
 }
 
 int dfs_state_set_classical(dfs_state s, uint64_t index) {
+    DFS_TRACE_CALL();
     int rc = check_state(s);
     if (rc) return rc;
     if (index >= s->numAmps) return fail(DFS_ERR_INVALID_ARG, "index %llu out of range", (unsigned long long)index);
@@ -421,6 +434,7 @@ int dfs_state_set_classical(dfs_state s, uint64_t index) {
 }
 
 int dfs_state_set_random(dfs_state s, uint64_t seed, int normalise) {
+    DFS_TRACE_CALL();
     int rc = check_state(s);
     return rc ? rc : state_set_random(s, seed, normalise);
 }
@@ -428,6 +442,7 @@ int dfs_state_set_random(dfs_state s, uint64_t seed, int normalise) {
 // ------------------------------------------------------ statevector gates
 
 int dfs_statevector_oneTargGate(dfs_state s, unsigned target, const double* gate) {
+    DFS_TRACE_CALL();
     int rc = check_state(s);
     if (!rc) rc = check_qubit(target, s->vecQubits, "target");
     if (!rc && !gate) rc = fail(DFS_ERR_INVALID_ARG, "null gate");
@@ -436,6 +451,7 @@ int dfs_statevector_oneTargGate(dfs_state s, unsigned target, const double* gate
 
 int dfs_statevector_manyCtrlOneTargGate(dfs_state s, const unsigned* controls, unsigned nc, unsigned target,
                                         const double* gate) {
+    DFS_TRACE_CALL();
     int rc = check_state(s);
     if (!rc) rc = check_qubit(target, s->vecQubits, "target");
     if (!rc) rc = check_list(controls, nc, s->vecQubits, "control", true);
@@ -448,6 +464,7 @@ int dfs_statevector_manyCtrlOneTargGate(dfs_state s, const unsigned* controls, u
 }
 
 int dfs_statevector_swapGate(dfs_state s, unsigned qb1, unsigned qb2) {
+    DFS_TRACE_CALL();
     int rc = check_state(s);
     if (!rc) rc = check_qubit(qb1, s->vecQubits, "qubit");
     if (!rc) rc = check_qubit(qb2, s->vecQubits, "qubit");
@@ -456,6 +473,7 @@ int dfs_statevector_swapGate(dfs_state s, unsigned qb1, unsigned qb2) {
 }
 
 int dfs_statevector_manyTargGate(dfs_state s, const unsigned* targets, unsigned k, const double* gate) {
+    DFS_TRACE_CALL();
     int rc = check_state(s);
     if (!rc) rc = check_list(targets, k, s->vecQubits, "target", false);
     if (!rc && !gate) rc = fail(DFS_ERR_INVALID_ARG, "null gate");
@@ -463,6 +481,7 @@ int dfs_statevector_manyTargGate(dfs_state s, const unsigned* targets, unsigned 
 }
 
 int dfs_statevector_pauliTensor(dfs_state s, const unsigned* targets, const unsigned* paulis, unsigned k) {
+    DFS_TRACE_CALL();
     int rc = check_state(s);
     if (!rc) rc = check_list(targets, k, s->vecQubits, "target", true);
     if (!rc) rc = check_paulis(paulis, k);
@@ -471,6 +490,7 @@ int dfs_statevector_pauliTensor(dfs_state s, const unsigned* targets, const unsi
 
 int dfs_statevector_pauliGadget(dfs_state s, const unsigned* targets, const unsigned* paulis, unsigned k,
                                 double theta) {
+    DFS_TRACE_CALL();
     int rc = check_state(s);
     if (!rc) rc = check_list(targets, k, s->vecQubits, "target", true);
     if (!rc) rc = check_paulis(paulis, k);
@@ -478,6 +498,7 @@ int dfs_statevector_pauliGadget(dfs_state s, const unsigned* targets, const unsi
 }
 
 int dfs_statevector_phaseGadget(dfs_state s, const unsigned* targets, unsigned k, double theta) {
+    DFS_TRACE_CALL();
     int rc = check_state(s);
     if (!rc) rc = check_list(targets, k, s->vecQubits, "target", true);
     return rc ? rc : sv_phase_gadget(s, targets, k, theta);
@@ -486,6 +507,7 @@ int dfs_statevector_phaseGadget(dfs_state s, const unsigned* targets, unsigned k
 // --------------------------------------------------------- density matrix
 
 int dfs_densitymatrix_manyTargGate(dfs_state s, const unsigned* targets, unsigned k, const double* gate) {
+    DFS_TRACE_CALL();
     int rc = check_dm(s);
     if (!rc) rc = check_list(targets, k, s->numQubits, "target", false);
     if (!rc && !gate) rc = fail(DFS_ERR_INVALID_ARG, "null gate");
@@ -516,6 +538,7 @@ int dfs_densitymatrix_manyTargGate(dfs_state s, const unsigned* targets, unsigne
 }
 
 int dfs_densitymatrix_swapGate(dfs_state s, unsigned qb1, unsigned qb2) {
+    DFS_TRACE_CALL();
     int rc = check_dm(s);
     if (!rc) rc = check_qubit(qb1, s->numQubits, "qubit");
     if (!rc) rc = check_qubit(qb2, s->numQubits, "qubit");
@@ -525,6 +548,7 @@ int dfs_densitymatrix_swapGate(dfs_state s, unsigned qb1, unsigned qb2) {
 }
 
 int dfs_densitymatrix_pauliTensor(dfs_state s, const unsigned* targets, const unsigned* paulis, unsigned k) {
+    DFS_TRACE_CALL();
     int rc = check_dm(s);
     if (!rc) rc = check_list(targets, k, s->numQubits, "target", true);
     if (!rc) rc = check_paulis(paulis, k);
@@ -537,6 +561,7 @@ int dfs_densitymatrix_pauliTensor(dfs_state s, const unsigned* targets, const un
 
 int dfs_densitymatrix_pauliGadget(dfs_state s, const unsigned* targets, const unsigned* paulis, unsigned k,
                                   double theta) {
+    DFS_TRACE_CALL();
     int rc = check_dm(s);
     if (!rc) rc = check_list(targets, k, s->numQubits, "target", true);
     if (!rc) rc = check_paulis(paulis, k);
@@ -547,6 +572,7 @@ int dfs_densitymatrix_pauliGadget(dfs_state s, const unsigned* targets, const un
 }
 
 int dfs_densitymatrix_phaseGadget(dfs_state s, const unsigned* targets, unsigned k, double theta) {
+    DFS_TRACE_CALL();
     int rc = check_dm(s);
     if (!rc) rc = check_list(targets, k, s->numQubits, "target", true);
     if (rc) return rc;
@@ -557,6 +583,7 @@ int dfs_densitymatrix_phaseGadget(dfs_state s, const unsigned* targets, unsigned
 
 int dfs_densitymatrix_krausMap(dfs_state s, const double* ops, unsigned numOps, const unsigned* targets,
                                unsigned k) {
+    DFS_TRACE_CALL();
     int rc = check_dm(s);
     if (!rc) rc = check_list(targets, k, s->numQubits, "target", false);
     if (!rc && (!ops || numOps == 0)) rc = fail(DFS_ERR_INVALID_ARG, "no Kraus operators given");
@@ -580,6 +607,7 @@ int dfs_densitymatrix_krausMap(dfs_state s, const double* ops, unsigned numOps, 
 }
 
 int dfs_densitymatrix_oneQubitDephasing(dfs_state s, unsigned qb, double prob) {
+    DFS_TRACE_CALL();
     int rc = check_dm(s);
     if (!rc) rc = check_qubit(qb, s->numQubits, "qubit");
     return rc ? rc : dm_deph1(s, qb, prob);
@@ -594,27 +622,32 @@ static int check_two(dfs_state s, unsigned q1, unsigned q2) {
 }
 
 int dfs_densitymatrix_twoQubitDephasing(dfs_state s, unsigned qb1, unsigned qb2, double prob) {
+    DFS_TRACE_CALL();
     int rc = check_two(s, qb1, qb2);
     return rc ? rc : dm_deph2(s, qb1, qb2, prob);
 }
 
 int dfs_densitymatrix_oneQubitDepolarising(dfs_state s, unsigned qb, double prob) {
+    DFS_TRACE_CALL();
     int rc = check_dm(s);
     if (!rc) rc = check_qubit(qb, s->numQubits, "qubit");
     return rc ? rc : dm_depol1(s, qb, prob);
 }
 
 int dfs_densitymatrix_twoQubitDepolarising(dfs_state s, unsigned qb1, unsigned qb2, double prob) {
+    DFS_TRACE_CALL();
     int rc = check_two(s, qb1, qb2);
     return rc ? rc : dm_depol2(s, qb1, qb2, prob, 0);
 }
 
 int dfs_densitymatrix_twoQubitDepolarising_referenceCompat(dfs_state s, unsigned qb1, unsigned qb2, double prob) {
+    DFS_TRACE_CALL();
     int rc = check_two(s, qb1, qb2);
     return rc ? rc : dm_depol2(s, qb1, qb2, prob, 1);
 }
 
 int dfs_densitymatrix_damping(dfs_state s, unsigned qb, double prob) {
+    DFS_TRACE_CALL();
     int rc = check_dm(s);
     if (!rc) rc = check_qubit(qb, s->numQubits, "qubit");
     return rc ? rc : dm_damping(s, qb, prob);
@@ -622,6 +655,7 @@ int dfs_densitymatrix_damping(dfs_state s, unsigned qb, double prob) {
 
 int dfs_densitymatrix_expecPauliString(dfs_state s, const double* coeffs, unsigned numTerms,
                                        const unsigned* allPaulis, double* re, double* im) {
+    DFS_TRACE_CALL();
     int rc = check_dm(s);
     if (!rc && (!re || !im)) rc = fail(DFS_ERR_INVALID_ARG, "null output");
     if (!rc && numTerms && (!coeffs || !allPaulis)) rc = fail(DFS_ERR_INVALID_ARG, "null term arrays");
@@ -636,6 +670,7 @@ int dfs_densitymatrix_expecPauliString(dfs_state s, const double* coeffs, unsign
 }
 
 int dfs_densitymatrix_partialTrace(dfs_state s, const unsigned* targets, unsigned k, dfs_state* out) {
+    DFS_TRACE_CALL();
     int rc = check_dm(s);
     if (!rc) rc = check_list(targets, k, s->numQubits, "target", true);
     if (!rc && !out) rc = fail(DFS_ERR_INVALID_ARG, "null output handle");
@@ -654,6 +689,7 @@ int dfs_densitymatrix_partialTrace(dfs_state s, const unsigned* targets, unsigne
 
 int dfs_statevector_expecPauliSum(dfs_state s, const double* coeffs, unsigned numTerms, const unsigned* allPaulis,
                                   double* re, double* im) {
+    DFS_TRACE_CALL();
     int rc = check_state(s);
     if (!rc && (!re || !im)) rc = fail(DFS_ERR_INVALID_ARG, "null output");
     if (!rc && numTerms && (!coeffs || !allPaulis)) rc = fail(DFS_ERR_INVALID_ARG, "null term arrays");
@@ -670,6 +706,7 @@ int dfs_statevector_expecPauliSum(dfs_state s, const double* coeffs, unsigned nu
 }
 
 int dfs_state_inner_product(dfs_state a, dfs_state b, double* re, double* im) {
+    DFS_TRACE_CALL();
     int rc = check_state(a);
     if (!rc) rc = check_state(b);
     if (!rc && (!re || !im)) rc = fail(DFS_ERR_INVALID_ARG, "null output");
@@ -680,12 +717,14 @@ int dfs_state_inner_product(dfs_state a, dfs_state b, double* re, double* im) {
 }
 
 int dfs_state_norm_squared(dfs_state s, double* out) {
+    DFS_TRACE_CALL();
     int rc = check_state(s);
     if (!rc && !out) rc = fail(DFS_ERR_INVALID_ARG, "null output");
     return rc ? rc : state_norm2(s, out);
 }
 
 int dfs_densitymatrix_trace(dfs_state s, double* re, double* im) {
+    DFS_TRACE_CALL();
     int rc = check_dm(s);
     if (!rc && (!re || !im)) rc = fail(DFS_ERR_INVALID_ARG, "null output");
     return rc ? rc : dm_trace(s, re, im);

@@ -454,6 +454,7 @@ using namespace dfs;
 extern "C" {
 
 int dfs_batch_create(const dfs_circuit* circuits, unsigned num, int precision, dfs_batch* out) {
+    DFS_TRACE_CALL();
     if (!out || !circuits || num == 0) return fail(DFS_ERR_INVALID_ARG, "empty batch or null output");
     if (precision != DFS_C128 && precision != DFS_C128_NATIVE && precision != DFS_C64)
         return fail(DFS_ERR_PRECISION, "unknown precision %d", precision);
@@ -503,6 +504,7 @@ static State arena_view(Batch* b, int arena, unsigned i) {
 }
 
 int dfs_batch_set_state(dfs_batch b, unsigned index, dfs_state s) {
+    DFS_TRACE_CALL();
     if (!b || !s) return fail(DFS_ERR_INVALID_ARG, "null batch or state");
     if (index >= b->num) return fail(DFS_ERR_INVALID_ARG, "circuit %u of %u", index, b->num);
     if (s->isDM || s->numQubits != b->nq[index]) return fail(DFS_ERR_STATE_KIND, "state does not match circuit %u", index);
@@ -517,6 +519,7 @@ int dfs_batch_set_state(dfs_batch b, unsigned index, dfs_state s) {
 }
 
 int dfs_batch_set_random(dfs_batch b, uint64_t seed) {
+    DFS_TRACE_CALL();
     if (!b) return fail(DFS_ERR_INVALID_ARG, "null batch");
     for (unsigned i = 0; i < b->num; i++) {
         State v = arena_view(b, 0, i);
@@ -528,6 +531,7 @@ int dfs_batch_set_random(dfs_batch b, uint64_t seed) {
 }
 
 int dfs_batch_get_state(dfs_batch b, unsigned index, dfs_state out) {
+    DFS_TRACE_CALL();
     if (!b || !out) return fail(DFS_ERR_INVALID_ARG, "null batch or state");
     if (index >= b->num) return fail(DFS_ERR_INVALID_ARG, "circuit %u of %u", index, b->num);
     if (out->isDM || out->numQubits != b->nq[index] || out->precision != b->precision)
@@ -543,6 +547,7 @@ int dfs_batch_get_state(dfs_batch b, unsigned index, dfs_state out) {
 
 int dfs_batch_set_hamiltonian(dfs_batch b, unsigned index, const double* coeffs, unsigned numTerms,
                               const unsigned* allPaulis) {
+    DFS_TRACE_CALL();
     if (!b) return fail(DFS_ERR_INVALID_ARG, "null batch");
     if (index >= b->num) return fail(DFS_ERR_INVALID_ARG, "circuit %u of %u", index, b->num);
     if (numTerms == 0 || numTerms > (unsigned)batch::kMaxTerms || !coeffs || !allPaulis)
@@ -572,6 +577,7 @@ int dfs_batch_set_hamiltonian(dfs_batch b, unsigned index, const double* coeffs,
 }
 
 int dfs_batch_set_params(dfs_batch b, const double* params) {
+    DFS_TRACE_CALL();
     if (!b) return fail(DFS_ERR_INVALID_ARG, "null batch");
     if (b->totalParams && !params) return fail(DFS_ERR_INVALID_ARG, "null parameters");
     // the graph copies the table from pinned memory: wait for a run in flight
@@ -608,6 +614,7 @@ int dfs_batch_get_shape(dfs_batch b, unsigned* ctasPerSM, unsigned* width) {
 }
 
 int dfs_batch_run(dfs_batch b, int withGradient, double* losses, double* grads) {
+    DFS_TRACE_CALL();
     if (!b) return fail(DFS_ERR_INVALID_ARG, "null batch");
     if (!has_all_terms(b)) return fail(DFS_ERR_INVALID_ARG, "every circuit needs a Hamiltonian");
     int rc = default_shape(b);
@@ -637,6 +644,7 @@ int dfs_batch_run(dfs_batch b, int withGradient, double* losses, double* grads) 
 }
 
 int dfs_batch_autotune(dfs_batch b, int withGradient, double* best_ms) {
+    DFS_TRACE_CALL();
     if (!b) return fail(DFS_ERR_INVALID_ARG, "null batch");
     if (!has_all_terms(b)) return fail(DFS_ERR_INVALID_ARG, "every circuit needs a Hamiltonian");
     int rc = upload_terms(b);
@@ -678,6 +686,7 @@ int dfs_batch_autotune(dfs_batch b, int withGradient, double* best_ms) {
 }
 
 int dfs_wait_selftest(double seconds, unsigned polls, int* spinTimedOut, int* mbarTimedOut) {
+    DFS_TRACE_CALL();
     if (!spinTimedOut || !mbarTimedOut) return fail(DFS_ERR_INVALID_ARG, "null output");
     if (!(seconds > 0 && seconds <= 10) || polls == 0)
         return fail(DFS_ERR_INVALID_ARG, "limits must be in (0, 10] seconds and > 0 polls");

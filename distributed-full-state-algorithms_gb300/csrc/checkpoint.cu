@@ -40,6 +40,7 @@ struct Pinned {
 }  // namespace
 
 static int save(dfs_state s, const char* path) {
+    DFS_TRACE_CALL();
     if (!path) return fail(DFS_ERR_INVALID_ARG, "null path");
     dfs_state_info info;
     int rc = dfs_state_get_info(s, &info);
@@ -72,6 +73,7 @@ static int save(dfs_state s, const char* path) {
 }
 
 static int load(const char* path, dfs_state* out) {
+    DFS_TRACE_CALL();
     if (!path || !out) return fail(DFS_ERR_INVALID_ARG, "null path or output handle");
     *out = nullptr;
     File file;

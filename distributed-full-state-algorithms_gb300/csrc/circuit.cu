@@ -751,6 +751,7 @@ using namespace dfs;
 extern "C" {
 
 int dfs_circuit_create(unsigned n, int isDM, dfs_circuit* out) {
+    DFS_TRACE_CALL();
     if (!out) return fail(DFS_ERR_INVALID_ARG, "null output");
     if (n == 0 || n > (unsigned)(isDM ? kMaxQubits / 2 : kMaxQubits))
         return fail(DFS_ERR_TOO_LARGE, "unsupported qubit count %u", n);
@@ -785,6 +786,7 @@ int dfs_circuit_num_params(dfs_circuit c, unsigned* out) {
 }
 
 int dfs_circuit_set_fusion(dfs_circuit c, int enable) {
+    DFS_TRACE_CALL();
     int rc = check_circuit(c);
     if (rc) return rc;
     c->fusion = enable != 0;
@@ -793,6 +795,7 @@ int dfs_circuit_set_fusion(dfs_circuit c, int enable) {
 }
 
 int dfs_circuit_fused_runs(dfs_circuit c, int precision, unsigned* runs, unsigned* fusedOps) {
+    DFS_TRACE_CALL();
     int rc = check_circuit(c);
     if (rc) return rc;
     if (!runs || !fusedOps) return fail(DFS_ERR_INVALID_ARG, "null output");
@@ -819,6 +822,7 @@ int dfs_circuit_num_ops(dfs_circuit c, unsigned* out) {
 }
 
 int dfs_circuit_oneTargGate(dfs_circuit c, unsigned target, const double* gate) {
+    DFS_TRACE_CALL();
     int rc = check_circuit(c);
     if (!rc) rc = check_q(c, target);
     if (!rc && !gate) rc = fail(DFS_ERR_INVALID_ARG, "null gate");
@@ -832,6 +836,7 @@ int dfs_circuit_oneTargGate(dfs_circuit c, unsigned target, const double* gate) 
 
 int dfs_circuit_manyCtrlOneTargGate(dfs_circuit c, const unsigned* ctrls, unsigned nc, unsigned target,
                                     const double* gate) {
+    DFS_TRACE_CALL();
     int rc = check_circuit(c);
     if (rc) return rc;
     std::vector<unsigned> all(ctrls, ctrls + (ctrls ? nc : 0));
@@ -847,6 +852,7 @@ int dfs_circuit_manyCtrlOneTargGate(dfs_circuit c, const unsigned* ctrls, unsign
 }
 
 int dfs_circuit_swapGate(dfs_circuit c, unsigned q1, unsigned q2) {
+    DFS_TRACE_CALL();
     int rc = check_circuit(c);
     if (!rc) rc = check_q(c, q1);
     if (!rc) rc = check_q(c, q2);
@@ -859,6 +865,7 @@ int dfs_circuit_swapGate(dfs_circuit c, unsigned q1, unsigned q2) {
 }
 
 int dfs_circuit_manyTargGate(dfs_circuit c, const unsigned* targs, unsigned k, const double* gate) {
+    DFS_TRACE_CALL();
     int rc = check_circuit(c);
     if (!rc) rc = check_qs(c, targs, k, false);
     if (!rc && !gate) rc = fail(DFS_ERR_INVALID_ARG, "null gate");
@@ -896,35 +903,44 @@ static int pauli_op(dfs_circuit c, OpKind kind, const unsigned* targs, const uns
 }
 
 int dfs_circuit_pauliTensor(dfs_circuit c, const unsigned* targs, const unsigned* paulis, unsigned k) {
+    DFS_TRACE_CALL();
     return pauli_op(c, OP_PAULI_TENSOR, targs, paulis, k, -1, 0.0);
 }
 
 int dfs_circuit_pauliGadget(dfs_circuit c, const unsigned* targs, const unsigned* paulis, unsigned k, int param,
                             double theta) {
+    DFS_TRACE_CALL();
     return pauli_op(c, OP_PAULI_GADGET, targs, paulis, k, param, theta);
 }
 
 int dfs_circuit_phaseGadget(dfs_circuit c, const unsigned* targs, unsigned k, int param, double theta) {
+    DFS_TRACE_CALL();
     return pauli_op(c, OP_PHASE_GADGET, targs, nullptr, k, param, theta);
 }
 
 int dfs_circuit_oneQubitDephasing(dfs_circuit c, unsigned qb, int param, double prob) {
+    DFS_TRACE_CALL();
     return add_channel(c, OP_DEPH1, {qb}, param, prob);
 }
 int dfs_circuit_twoQubitDephasing(dfs_circuit c, unsigned qb1, unsigned qb2, int param, double prob) {
+    DFS_TRACE_CALL();
     return add_channel(c, OP_DEPH2, {qb1, qb2}, param, prob);
 }
 int dfs_circuit_oneQubitDepolarising(dfs_circuit c, unsigned qb, int param, double prob) {
+    DFS_TRACE_CALL();
     return add_channel(c, OP_DEPOL1, {qb}, param, prob);
 }
 int dfs_circuit_twoQubitDepolarising(dfs_circuit c, unsigned qb1, unsigned qb2, int param, double prob) {
+    DFS_TRACE_CALL();
     return add_channel(c, OP_DEPOL2, {qb1, qb2}, param, prob);
 }
 int dfs_circuit_damping(dfs_circuit c, unsigned qb, int param, double prob) {
+    DFS_TRACE_CALL();
     return add_channel(c, OP_DAMPING, {qb}, param, prob);
 }
 
 int dfs_circuit_apply(dfs_circuit c, dfs_state s, const double* params) {
+    DFS_TRACE_CALL();
     int rc = check_circuit(c);
     if (!rc) rc = check_state_for(c, s);
     if (!rc) rc = check_params(c, params);
@@ -934,6 +950,7 @@ int dfs_circuit_apply(dfs_circuit c, dfs_state s, const double* params) {
 
 int dfs_circuit_expec(dfs_circuit c, dfs_state initial, const double* params, const double* coeffs,
                       unsigned numTerms, const unsigned* allPaulis, double* loss) {
+    DFS_TRACE_CALL();
     int rc = check_circuit(c);
     if (!rc) rc = check_state_for(c, initial);
     if (!rc) rc = check_params(c, params);
@@ -977,6 +994,7 @@ int dfs_circuit_expec(dfs_circuit c, dfs_state initial, const double* params, co
 }
 
 int dfs_circuit_gradient(dfs_circuit c, const double* params, double* grad) {
+    DFS_TRACE_CALL();
     int rc = check_circuit(c);
     if (!rc) rc = check_params(c, params);
     if (!rc && c->numParams > 0 && !grad) rc = fail(DFS_ERR_INVALID_ARG, "null gradient output");

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <vector>
@@ -50,6 +51,16 @@ struct State {
 
 // orders the context stream after the state's pending asynchronous transfer
 int state_acquire(State* s);
+
+// an NVTX range over one API call, named after the entry point (shown by Nsight Systems
+// and `ncu --nvtx`; a pointer test when no tool is attached)
+struct TraceRange {
+    explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+    ~TraceRange() { nvtxRangePop(); }
+    TraceRange(const TraceRange&) = delete;
+    TraceRange& operator=(const TraceRange&) = delete;
+};
+#define DFS_TRACE_CALL() ::dfs::TraceRange dfsTraceRange_(__func__)
 
 // records a message for dfs_last_error and returns code
 int fail(int code, const char* fmt, ...);
