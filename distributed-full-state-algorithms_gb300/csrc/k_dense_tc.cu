@@ -14,11 +14,11 @@
 //    transformation of matrix multiplication by using fast routines of matrix
 //    multiplication and its applications", Numer. Algorithms 59 (2012)).  Every
 //    real of a group is scaled by the group's largest power of two and cut into
-//    six 8-bit integer slices (48 bits), each an exact bf16; every gate row is
-//    cut the same way with its own power of two.  A slice product summed over
-//    K <= 64 terms is an integer below 2^22, and the accumulators of weights
-//    2^0 .. 2^-24 (1 to 4 products) stay below 2^24, so the FP32 tensor-core
-//    accumulation is exact there.
+//    six balanced 8-bit digits (|d| <= 192, split_digits), each an exact bf16;
+//    every gate row is cut into six unsigned bytes with its own power of two.  A
+//    digit product summed over K <= 64 terms is an integer below 2^21.6, and the
+//    accumulators of weights 2^0 .. 2^-24 (1 to 4 products) stay below 2^24, so
+//    the FP32 tensor-core accumulation is exact there.
 //    The 21 products with s + t <= 5 go to five TMEM accumulators (the two
 //    lowest weights share one, with B pre-scaled); the epilogue sums them in
 //    double-float (two exact TwoSums, the rest into the error term) and rounds
@@ -79,15 +79,48 @@ struct DenseParams {
 
 // ------------------------------------------------------------ complex128
 
-// double bits -> (sign, 48-bit fraction relative to 2^(E - 1022)) for the group's
-// largest biased exponent E
-DEV uint64_t fraction48(uint32_t H, uint32_t L, uint32_t E) {
-    uint32_t ex = (H >> 20) & 0x7FFu;
-    uint64_t M = ((uint64_t)((H & 0xFFFFFu) | 0x100000u) << 32) | L;
-    uint32_t sh = E - ex + 5u;
-    uint64_t F = sh < 64u ? (M >> sh) : 0ull;
-    return ex == 0u ? 0ull : F;
+// The six digits of an amplitude (re, im as an f32x2 pair per digit) for a group whose
+// largest biased exponent is E: X = x 2^(1069 - E) (|X| < 2^47) in balanced digits d_s of
+// weight 2^(40 - 8s), made on the FP32 pipe.  The double splits exactly into hi (the top
+// 24 bits of its significand, with the exponent rebiased by E: cE = ((173 - E) mod 256)
+// << 23 added to the float exponent field) and lo (the next 23 bits, truncated); then
+// d = rint(r 2^-w) by adding and subtracting 1.5 * 2^23, and r -= d 2^w exactly, lo
+// joining the remainder after the third digit.  |d_s| <= 128 except |d_3| <= 192 (hi's
+// remainder plus lo), all exact in bf16.  Zeros and values below 2^-93 of the group's
+// largest (ex < E - 140) give zero digits; the truncated bits and the rounding of the
+// remainder cost at most one unit of the last digit, 2^-46 of the largest amplitude.
+DEV void split_digits(uint4 v, uint32_t E, uint32_t cE, uint64_t (&d)[kOzSlices]) {
+    auto rebias = [&](uint32_t H, uint32_t L, float& hi, float& lo) {
+        const uint32_t ex = (H >> 20) & 0x7FFu;
+        const uint32_t hb = ((__funnelshift_l(L, H, 3) + cE) & 0x7FFFFFFFu) | (H & 0x80000000u);
+        const uint32_t mb = (hb & 0xFF800000u) - (23u << 23);  // +-2^(e_hi - 23): ulp 2^(e_hi - 46)
+        const float l = __fsub_rn(__uint_as_float(mb | ((L >> 6) & 0x7FFFFFu)), __uint_as_float(mb));
+        const bool zero = ex == 0u || ex + 140u < E;
+        hi = zero ? 0.f : __uint_as_float(hb);
+        lo = zero ? 0.f : l;
+    };
+    float hr, lr, hm, lm;
+    rebias(v.y, v.x, hr, lr);
+    rebias(v.w, v.z, hm, lm);
+    const uint64_t M = tc::pk2(0x1.8p23f, 0x1.8p23f);
+    uint64_t r = tc::pk2(hr, hm);
+    d[0] = tc::sub2(tc::fma2(r, tc::pk2(0x1p-40f, 0x1p-40f), M), M);
+    r = tc::fma2(d[0], tc::pk2(-0x1p40f, -0x1p40f), r);
+    d[1] = tc::sub2(tc::fma2(r, tc::pk2(0x1p-32f, 0x1p-32f), M), M);
+    r = tc::fma2(d[1], tc::pk2(-0x1p32f, -0x1p32f), r);
+    d[2] = tc::sub2(tc::fma2(r, tc::pk2(0x1p-24f, 0x1p-24f), M), M);
+    r = tc::fma2(d[2], tc::pk2(-0x1p24f, -0x1p24f), r);
+    r = tc::add2(r, tc::pk2(lr, lm));
+    d[3] = tc::sub2(tc::fma2(r, tc::pk2(0x1p-16f, 0x1p-16f), M), M);
+    r = tc::fma2(d[3], tc::pk2(-0x1p16f, -0x1p16f), r);
+    d[4] = tc::sub2(tc::fma2(r, tc::pk2(0x1p-8f, 0x1p-8f), M), M);
+    r = tc::fma2(d[4], tc::pk2(-0x1p8f, -0x1p8f), r);
+    d[5] = tc::sub2(tc::add2(r, M), M);
 }
+
+// the digits' scale: sum_s d_s 2^(40 - 8s) = X = x 2^(1069 - E), and the gate rows' bytes
+// b_t 2^(40 - 8t) = g 2^(48 - F_n), so y = 2^(E + F_n - 1037) sum_u D_u 2^(-8u)
+constexpr int kOzShift = 1037;
 
 // the bf16 halves of two floats packed as (lo, hi)
 DEV uint32_t pack_bf16(float lo, float hi) { return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632u); }
@@ -143,39 +176,20 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
         halfMax[half][row] = E;
         __syncthreads();
         E = max(E, halfMax[half ^ 1][row]);
+        const uint32_t cE = ((173u - E) & 0xFFu) << 23;
 
-        // ---- six 8-bit slices of this half's D reals, 8 reals (one core row) at a time
+        // ---- six digits of this half's D reals, 8 reals (one core row) at a time
 #pragma unroll
         for (int kg = 0; kg < D / 8; kg++) {
             uint32_t packed[kOzSlices][4];
 #pragma unroll
-            for (int j = 0; j < 4; j++) {  // amplitude kg*4 + j: reals (re, im), sliced as a pair
-                const uint4 v = cur[kg * 4 + j];
-                const uint64_t F0 = fraction48(v.y, v.x, E), F1 = fraction48(v.w, v.z, E);
-                const uint32_t Fh0 = (uint32_t)(F0 >> 32), Fl0 = (uint32_t)F0;
-                const uint32_t Fh1 = (uint32_t)(F1 >> 32), Fl1 = (uint32_t)F1;
-                const uint32_t mb0 = (v.y >> 31) ? 0xCB000000u : 0x4B000000u;
-                const uint32_t mb1 = (v.w >> 31) ? 0xCB000000u : 0x4B000000u;
-                const uint64_t magic = tc::pk2(__uint_as_float(mb0), __uint_as_float(mb1));
-                // sign * byte as an exact float: the byte under the exponent of +-2^23
-                // (one PRMT per real), minus +-2^23 (one f32x2 subtraction per pair)
-                uint32_t m0[kOzSlices], m1[kOzSlices];
-                m0[0] = __byte_perm(Fh0, mb0, 0x7651u);
-                m0[1] = __byte_perm(Fh0, mb0, 0x7650u);
-                m0[2] = __byte_perm(Fl0, mb0, 0x7653u);
-                m0[3] = __byte_perm(Fl0, mb0, 0x7652u);
-                m0[4] = __byte_perm(Fl0, mb0, 0x7651u);
-                m0[5] = __byte_perm(Fl0, mb0, 0x7650u);
-                m1[0] = __byte_perm(Fh1, mb1, 0x7651u);
-                m1[1] = __byte_perm(Fh1, mb1, 0x7650u);
-                m1[2] = __byte_perm(Fl1, mb1, 0x7653u);
-                m1[3] = __byte_perm(Fl1, mb1, 0x7652u);
-                m1[4] = __byte_perm(Fl1, mb1, 0x7651u);
-                m1[5] = __byte_perm(Fl1, mb1, 0x7650u);
+            for (int j = 0; j < 4; j++) {  // amplitude kg*4 + j: reals (re, im), split as a pair
+                uint64_t d[kOzSlices];
+                split_digits(cur[kg * 4 + j], E, cE, d);
 #pragma unroll
                 for (int sl = 0; sl < kOzSlices; sl++) {
                     float re, im;
-                    tc::up2(tc::sub2(tc::pk2(__uint_as_float(m0[sl]), __uint_as_float(m1[sl])), magic), re, im);
+                    tc::up2(d[sl], re, im);
                     packed[sl][j] = pack_bf16(re, im);
                 }
             }
@@ -223,7 +237,7 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
         }
         tc::fence_after_sync();
 
-        // ---- y_n = 2^(E + e_n - 1038) * sum_u D_u[n] 2^(-8u), summed in double-float: D_0,
+        // ---- y_n = 2^(E + e_n - kOzShift) * sum_u D_u[n] 2^(-8u), summed in double-float: D_0,
         //      D_1 2^-8 and D_2 2^-16 exactly (TwoSum), the rest into the error term
         // in chunks of 8 output reals (4 amplitudes) so that large D stays in registers
         const uint32_t lane = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(half * D);
@@ -258,10 +272,10 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
                     df::f2 yr, yi;
                     tc::up2(y, yr.hi, yi.hi);
                     tc::up2(yl, yr.lo, yi.lo);
-                    // times 2^(E + e_n - 1038), folded into the exponent field
+                    // times 2^(E + e_n - kOzShift), folded into the exponent field
                     uint32_t w[4];
-                    df::encode_words_scaled(yr, (int)E + p.colExp[half * D + 2 * c] - 1038, &w[1], &w[0]);
-                    df::encode_words_scaled(yi, (int)E + p.colExp[half * D + 2 * c + 1] - 1038, &w[3], &w[2]);
+                    df::encode_words_scaled(yr, (int)E + p.colExp[half * D + 2 * c] - kOzShift, &w[1], &w[0]);
+                    df::encode_words_scaled(yi, (int)E + p.colExp[half * D + 2 * c + 1] - kOzShift, &w[3], &w[2]);
                     amps[base + p.off[half * kHalf + c]] = make_uint4(w[0], w[1], w[2], w[3]);
                 }
             }
@@ -364,32 +378,15 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
             unsigned char* sA = smem + b * kOzSlices * S::A16;
             {
                 uint32_t packed[kOzSlices][4];
+                const uint32_t cE = ((173u - E) & 0xFFu) << 23;
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
-                    const uint4 v = cur[j];
-                    const uint64_t F0 = fraction48(v.y, v.x, E), F1 = fraction48(v.w, v.z, E);
-                    const uint32_t Fh0 = (uint32_t)(F0 >> 32), Fl0 = (uint32_t)F0;
-                    const uint32_t Fh1 = (uint32_t)(F1 >> 32), Fl1 = (uint32_t)F1;
-                    const uint32_t mb0 = (v.y >> 31) ? 0xCB000000u : 0x4B000000u;
-                    const uint32_t mb1 = (v.w >> 31) ? 0xCB000000u : 0x4B000000u;
-                    const uint64_t magic = tc::pk2(__uint_as_float(mb0), __uint_as_float(mb1));
-                    uint32_t m0[kOzSlices], m1[kOzSlices];
-                    m0[0] = __byte_perm(Fh0, mb0, 0x7651u);
-                    m0[1] = __byte_perm(Fh0, mb0, 0x7650u);
-                    m0[2] = __byte_perm(Fl0, mb0, 0x7653u);
-                    m0[3] = __byte_perm(Fl0, mb0, 0x7652u);
-                    m0[4] = __byte_perm(Fl0, mb0, 0x7651u);
-                    m0[5] = __byte_perm(Fl0, mb0, 0x7650u);
-                    m1[0] = __byte_perm(Fh1, mb1, 0x7651u);
-                    m1[1] = __byte_perm(Fh1, mb1, 0x7650u);
-                    m1[2] = __byte_perm(Fl1, mb1, 0x7653u);
-                    m1[3] = __byte_perm(Fl1, mb1, 0x7652u);
-                    m1[4] = __byte_perm(Fl1, mb1, 0x7651u);
-                    m1[5] = __byte_perm(Fl1, mb1, 0x7650u);
+                    uint64_t d[kOzSlices];
+                    split_digits(cur[j], E, cE, d);
 #pragma unroll
                     for (int sl = 0; sl < kOzSlices; sl++) {
                         float re, im;
-                        tc::up2(tc::sub2(tc::pk2(__uint_as_float(m0[sl]), __uint_as_float(m1[sl])), magic), re, im);
+                        tc::up2(d[sl], re, im);
                         packed[sl][j] = pack_bf16(re, im);
                     }
                 }
@@ -451,8 +448,8 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
                         tc::up2(y, yr.hi, yi.hi);
                         tc::up2(yl, yr.lo, yi.lo);
                         uint32_t w[4];
-                        df::encode_words_scaled(yr, (int)E + p.colExp[2 * c] - 1038, &w[1], &w[0]);
-                        df::encode_words_scaled(yi, (int)E + p.colExp[2 * c + 1] - 1038, &w[3], &w[2]);
+                        df::encode_words_scaled(yr, (int)E + p.colExp[2 * c] - kOzShift, &w[1], &w[0]);
+                        df::encode_words_scaled(yi, (int)E + p.colExp[2 * c + 1] - kOzShift, &w[3], &w[2]);
                         amps[base + p.off[c]] = make_uint4(w[0], w[1], w[2], w[3]);
                     }
                 }
