@@ -281,6 +281,22 @@ def apply(dfs, state, gates: Sequence[Gate]) -> None:
             raise ValueError(f"unknown gate kind {k}")
 
 
+def inverse(gates: Sequence[Gate]) -> list[Gate]:
+    """The inverse circuit of unitary gates: reverse order, adjoint matrices, negated
+    angles (a swap and a Pauli tensor are their own inverses)."""
+    out = []
+    for g in reversed(gates):
+        if g.kind in ("one_targ", "ctrl", "many_targ"):
+            out.append(Gate(g.kind, g.qubits, g.controls, np.conj(np.asarray(g.matrix)).T.copy(), g.paulis, g.param))
+        elif g.kind in ("pauli_gadget", "phase_gadget"):
+            out.append(Gate(g.kind, g.qubits, g.controls, g.matrix, g.paulis, -g.param))
+        elif g.kind in ("swap", "pauli_tensor"):
+            out.append(g)
+        else:
+            raise ValueError(f"{g.kind} is not a unitary gate")
+    return out
+
+
 def controlled(matrix: np.ndarray, num_controls: int) -> np.ndarray:
     """The dense matrix of a gate with controls, on targets (target, controls...):
     local index bit 0 addresses the target; identity unless every control bit is 1."""

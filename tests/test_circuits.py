@@ -52,3 +52,17 @@ def test_algorithmic_bytes(circuits):
     assert circuits.algorithmic_bytes(g, N, B) == 2 * N * B
     assert circuits.algorithmic_bytes(circuits.Gate("ctrl", (1,), controls=(2, 3)), N, B) == 2 * N * B // 4
     assert circuits.algorithmic_bytes(circuits.Gate("swap", (1, 2)), N, B) == N * B
+
+
+def test_inverse_circuit_round_trip(circuits, oracle):
+    """circuits.inverse undoes the gate mix (with dense gates) on the oracle."""
+    rng = np.random.default_rng(3)
+    for n in (5, 8):
+        gates = circuits.gate_mix(n, 60, seed=n, dense_k=(2, 3))
+        gates.insert(7, circuits.Gate("pauli_tensor", (0, 2), paulis=(2, 1)))
+        a = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+        b = a.copy()
+        circuits.apply_to(oracle, b, gates)
+        assert np.max(np.abs(b - a)) > 1e-3
+        circuits.apply_to(oracle, b, circuits.inverse(gates))
+        assert np.max(np.abs(b - a)) <= 1e-12 * np.max(np.abs(a))

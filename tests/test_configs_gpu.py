@@ -60,6 +60,30 @@ def test_density_matrix_workflow_12_qubits(dfs, oracle):
     assert abs(dfs.densitymatrix_trace(rho) - 1.0) <= 1e-12
 
 
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-11), ("c64", 5e-5)])
+def test_gate_mix_round_trip_30_qubits(dfs, prec, tol):
+    """The benchmark's own state and circuit (30 qubits, 200 gates of the mix): the norm is
+    kept, and the inverse circuit returns the initial state; at this size the oracle
+    would take hours, so the properties stand in for it."""
+    n = 30
+    gates = circuits.gate_mix(n, 200, seed=20240611)
+    psi = dfs.StateVector(n, precision=prec)
+    psi.setRandomAmps(seed=1, normalise=True)
+    init = dfs.StateVector(n, precision=prec)
+    init.copyFrom(psi)
+    circuits.apply(dfs, psi, gates)
+    assert abs(dfs.norm_squared(psi) - 1.0) <= tol
+    assert abs(dfs.inner_product(init, psi)) < 0.5  # the circuit did move the state
+    circuits.apply(dfs, psi, circuits.inverse(gates))
+    ip = dfs.inner_product(init, psi)
+    assert abs(ip - 1.0) <= tol
+    # amplitude-wise: 1 - |<init|psi>|^2 bounds the squared 2-norm distance
+    dist2 = dfs.norm_squared(psi) + dfs.norm_squared(init) - 2 * ip.real
+    assert dist2 <= tol
+    psi.free()
+    init.free()
+
+
 def test_precision_form_properties_26_qubits(dfs):
     n = 26
     gates = circuits.gate_mix(n, 60, seed=5, dense_k=(2, 4, 5, 6))
