@@ -30,6 +30,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "kernels.cuh"
@@ -75,6 +76,7 @@ struct DenseParams {
     QList q;                  // targets, sorted
     IT off[1 << KT];          // local index -> amplitude offset (bit i <-> targets[i])
     int colExp[2 << KT];      // complex128 path: per output real, the power of two of its gate row
+    int fastE;                // complex128 path: groups with E >= fastE give normal doubles only
 };
 
 // ------------------------------------------------------------ complex128
@@ -87,21 +89,20 @@ struct DenseParams {
 // d = rint(r 2^-w) by adding and subtracting 1.5 * 2^23, and r -= d 2^w exactly, lo
 // joining the remainder after the third digit.  |d_s| <= 128 except |d_3| <= 192 (hi's
 // remainder plus lo), all exact in bf16.  Zeros and values below 2^-93 of the group's
-// largest (ex < E - 140) give zero digits; the truncated bits and the rounding of the
-// remainder cost at most one unit of the last digit, 2^-46 of the largest amplitude.
-DEV void split_digits(uint4 v, uint32_t E, uint32_t cE, uint64_t (&d)[kOzSlices]) {
-    auto rebias = [&](uint32_t H, uint32_t L, float& hi, float& lo) {
-        const uint32_t ex = (H >> 20) & 0x7FFu;
+// largest (zr, zm: see digits_dropped) give zero digits; the truncated bits and the
+// rounding of the remainder cost at most one unit of the last digit, 2^-46 of the largest
+// amplitude.
+DEV void split_digits(uint4 v, bool zr, bool zm, uint32_t cE, uint64_t (&d)[kOzSlices]) {
+    auto rebias = [&](uint32_t H, uint32_t L, bool zero, float& hi, float& lo) {
         const uint32_t hb = ((__funnelshift_l(L, H, 3) + cE) & 0x7FFFFFFFu) | (H & 0x80000000u);
         const uint32_t mb = (hb & 0xFF800000u) - (23u << 23);  // +-2^(e_hi - 23): ulp 2^(e_hi - 46)
         const float l = __fsub_rn(__uint_as_float(mb | ((L >> 6) & 0x7FFFFFu)), __uint_as_float(mb));
-        const bool zero = ex == 0u || ex + 140u < E;
         hi = zero ? 0.f : __uint_as_float(hb);
         lo = zero ? 0.f : l;
     };
     float hr, lr, hm, lm;
-    rebias(v.y, v.x, hr, lr);
-    rebias(v.w, v.z, hm, lm);
+    rebias(v.y, v.x, zr, hr, lr);
+    rebias(v.w, v.z, zm, hm, lm);
     const uint64_t M = tc::pk2(0x1.8p23f, 0x1.8p23f);
     uint64_t r = tc::pk2(hr, hm);
     d[0] = tc::sub2(tc::fma2(r, tc::pk2(0x1p-40f, 0x1p-40f), M), M);
@@ -118,9 +119,35 @@ DEV void split_digits(uint4 v, uint32_t E, uint32_t cE, uint64_t (&d)[kOzSlices]
     d[5] = tc::sub2(tc::add2(r, M), M);
 }
 
+// The exponent field of a double's high word in place (ex << 20), and the group's bound
+// below which a real gets zero digits: ex == 0 (zero or subnormal) or ex < E - 140, for the
+// group's largest field E32 = E << 20, as one unsigned comparison of fields.
+DEV uint32_t exp_field(uint32_t H) { return H & 0x7FF00000u; }
+DEV uint32_t digits_dropped_below(uint32_t E32) { return (uint32_t)max((int)E32 - (140 << 20), 1 << 20); }
+
 // the digits' scale: sum_s d_s 2^(40 - 8s) = X = x 2^(1069 - E), and the gate rows' bytes
 // b_t 2^(40 - 8t) = g 2^(48 - F_n), so y = 2^(E + F_n - 1037) sum_u D_u 2^(-8u)
 constexpr int kOzShift = 1037;
+
+// Output y = hi + lo (a double-float with |lo| <= ulp(hi) / 2) as the double y 2^(ebias -
+// 896), rowcol = ebias << 20, for the sums of the accumulators: hi is zero or a multiple of
+// 2^-40 (every accumulator holds multiples of 2^-8, the lowest weight is 2^-32), so its
+// exponent field is >= 87 and the double is normal whenever ebias >= -86, which the host
+// guarantees through DenseParams::fastE.  As df::encode_words_scaled without the checks
+// for tiny and subnormal results: hi's bits give the high 24 bits, lo rounded to units of
+// the double's last place is added as an integer (twice when hi is a power of two and lo
+// negative, where the unit halves).
+DEV void encode_normal(float hi, float lo, uint32_t rowcol, uint32_t& Hw, uint32_t& Lw) {
+    const uint32_t hb = __float_as_uint(hi);
+    const uint32_t Hh = ((hb & 0x7FFFFFFFu) >> 3) + rowcol;
+    const uint32_t Lh = hb << 29;
+    const uint32_t sb = (306u << 23) - (hb & 0xFF800000u);  // +-2^(52 - e_hi) with hi's sign folded in
+    int32_t off = __float2int_rn(lo * __uint_as_float(sb));
+    if ((hb << 9) == 0u && off < 0) off += off;
+    const uint64_t bits = ((((uint64_t)Hh) << 32) | Lh) + (uint64_t)(int64_t)off;
+    Hw = hi == 0.f ? (hb & 0x80000000u) : ((uint32_t)(bits >> 32) | (hb & 0x80000000u));
+    Lw = hi == 0.f ? 0u : (uint32_t)bits;
+}
 
 // the bf16 halves of two floats packed as (lo, hi)
 DEV uint32_t pack_bf16(float lo, float hi) { return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632u); }
@@ -170,12 +197,13 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
         const IT base = valid ? insert_zeros(g, p.q) : (IT)0;
 
         // ---- the group's largest exponent (both halves)
-        uint32_t E = 0;
+        uint32_t E32 = 0;
 #pragma unroll
-        for (int c = 0; c < kHalf; c++) E = max(E, max((cur[c].y >> 20) & 0x7FFu, (cur[c].w >> 20) & 0x7FFu));
-        halfMax[half][row] = E;
+        for (int c = 0; c < kHalf; c++) E32 = max(E32, max(exp_field(cur[c].y), exp_field(cur[c].w)));
+        halfMax[half][row] = E32;
         __syncthreads();
-        E = max(E, halfMax[half ^ 1][row]);
+        E32 = max(E32, halfMax[half ^ 1][row]);
+        const uint32_t E = E32 >> 20, thr = digits_dropped_below(E32);
         const uint32_t cE = ((173u - E) & 0xFFu) << 23;
 
         // ---- six digits of this half's D reals, 8 reals (one core row) at a time
@@ -184,8 +212,9 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
             uint32_t packed[kOzSlices][4];
 #pragma unroll
             for (int j = 0; j < 4; j++) {  // amplitude kg*4 + j: reals (re, im), split as a pair
+                const uint4 v = cur[kg * 4 + j];
                 uint64_t d[kOzSlices];
-                split_digits(cur[kg * 4 + j], E, cE, d);
+                split_digits(v, exp_field(v.y) < thr, exp_field(v.w) < thr, cE, d);
 #pragma unroll
                 for (int sl = 0; sl < kOzSlices; sl++) {
                     float re, im;
@@ -369,11 +398,12 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
             const int b = i & 1;
             const uint32_t k = (uint32_t)i >> 1;
             if (i >= 2 && !(ok = tc::mbar_wait(&accFree[b], (k - 1) & 1, kTcWaitLimit))) break;
-            uint32_t E = 0;
+            uint32_t E32 = 0;
 #pragma unroll
-            for (int c = 0; c < H; c++) E = max(E, max((cur[c].y >> 20) & 0x7FFu, (cur[c].w >> 20) & 0x7FFu));
+            for (int c = 0; c < H; c++) E32 = max(E32, max(exp_field(cur[c].y), exp_field(cur[c].w)));
 #pragma unroll
-            for (int m = 1; m < W::SPR; m <<= 1) E = max(E, __shfl_xor_sync(0xffffffffu, E, m));
+            for (int m = 1; m < W::SPR; m <<= 1) E32 = max(E32, __shfl_xor_sync(0xffffffffu, E32, m));
+            const uint32_t E = E32 >> 20, thr = digits_dropped_below(E32);
             if (part == 0) sE[b][row] = E;
             unsigned char* sA = smem + b * kOzSlices * S::A16;
             {
@@ -382,7 +412,7 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     uint64_t d[kOzSlices];
-                    split_digits(cur[j], E, cE, d);
+                    split_digits(cur[j], exp_field(cur[j].y) < thr, exp_field(cur[j].w) < thr, cE, d);
 #pragma unroll
                     for (int sl = 0; sl < kOzSlices; sl++) {
                         float re, im;
@@ -419,41 +449,54 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
             const bool valid = g < numGroups;
             const IT base = valid ? insert_zeros(g, p.q) : (IT)0;
             const uint32_t lanes = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)b * W::kAccCols;
+            const uint32_t rowc = (uint32_t)((int)E + 896 - kOzShift) << 20;
+            // the whole warp's results are normal doubles (the usual case) or it takes the
+            // general encoding; one instantiation each keeps both free of the other's branches
+            auto drain_tile = [&](auto normalTag) {
+                constexpr bool kNormal = decltype(normalTag)::value;
 #pragma unroll
-            for (int ch = cg; ch < D / 4; ch += W::EPQ) {
-                float acc[kOzAccs][8];
+                for (int ch = cg; ch < D / 4; ch += W::EPQ) {
+                    float acc[kOzAccs][8];
 #pragma unroll
-                for (int u = 0; u < kOzAccs; u++) {
-                    float v[16];
-                    tc::ld8(lanes + (uint32_t)(u * R + ch * 8), v);
+                    for (int u = 0; u < kOzAccs; u++) {
+                        float v[16];
+                        tc::ld8(lanes + (uint32_t)(u * R + ch * 8), v);
 #pragma unroll
-                    for (int j = 0; j < 8; j++) acc[u][j] = v[j];
-                }
-                tc::ld_wait();
-                if (valid) {
+                        for (int j = 0; j < 8; j++) acc[u][j] = v[j];
+                    }
+                    tc::ld_wait();
+                    if (valid) {
 #pragma unroll
-                    for (int c4 = 0; c4 < 4; c4++) {
-                        const int c = ch * 4 + c4;
-                        uint64_t a[kOzAccs];
+                        for (int c4 = 0; c4 < 4; c4++) {
+                            const int c = ch * 4 + c4;
+                            uint64_t a[kOzAccs];
 #pragma unroll
-                        for (int u = 0; u < kOzAccs; u++) a[u] = tc::pk2(acc[u][2 * c4], acc[u][2 * c4 + 1]);
-                        uint64_t t, tl, t2, t2l, y, yl;
-                        tc::two_sum2(a[0], tc::mul2(a[1], tc::pk2(0x1p-8f, 0x1p-8f)), t, tl);
-                        tc::two_sum2(t, tc::mul2(a[2], tc::pk2(0x1p-16f, 0x1p-16f)), t2, t2l);
-                        uint64_t e = tc::add2(tl, t2l);
-                        e = tc::fma2(a[3], tc::pk2(0x1p-24f, 0x1p-24f), e);
-                        e = tc::fma2(a[4], tc::pk2(0x1p-32f, 0x1p-32f), e);
-                        tc::fast_two_sum2(t2, e, y, yl);
-                        df::f2 yr, yi;
-                        tc::up2(y, yr.hi, yi.hi);
-                        tc::up2(yl, yr.lo, yi.lo);
-                        uint32_t w[4];
-                        df::encode_words_scaled(yr, (int)E + p.colExp[2 * c] - kOzShift, &w[1], &w[0]);
-                        df::encode_words_scaled(yi, (int)E + p.colExp[2 * c + 1] - kOzShift, &w[3], &w[2]);
-                        amps[base + p.off[c]] = make_uint4(w[0], w[1], w[2], w[3]);
+                            for (int u = 0; u < kOzAccs; u++) a[u] = tc::pk2(acc[u][2 * c4], acc[u][2 * c4 + 1]);
+                            uint64_t t, tl, t2, t2l, y, yl;
+                            tc::two_sum2(a[0], tc::mul2(a[1], tc::pk2(0x1p-8f, 0x1p-8f)), t, tl);
+                            tc::two_sum2(t, tc::mul2(a[2], tc::pk2(0x1p-16f, 0x1p-16f)), t2, t2l);
+                            uint64_t e = tc::add2(tl, t2l);
+                            e = tc::fma2(a[3], tc::pk2(0x1p-24f, 0x1p-24f), e);
+                            e = tc::fma2(a[4], tc::pk2(0x1p-32f, 0x1p-32f), e);
+                            tc::fast_two_sum2(t2, e, y, yl);
+                            df::f2 yr, yi;
+                            tc::up2(y, yr.hi, yi.hi);
+                            tc::up2(yl, yr.lo, yi.lo);
+                            uint32_t w[4];
+                            if constexpr (kNormal) {
+                                encode_normal(yr.hi, yr.lo, rowc + ((uint32_t)p.colExp[2 * c] << 20), w[1], w[0]);
+                                encode_normal(yi.hi, yi.lo, rowc + ((uint32_t)p.colExp[2 * c + 1] << 20), w[3], w[2]);
+                            } else {
+                                df::encode_words_scaled(yr, (int)E + p.colExp[2 * c] - kOzShift, &w[1], &w[0]);
+                                df::encode_words_scaled(yi, (int)E + p.colExp[2 * c + 1] - kOzShift, &w[3], &w[2]);
+                            }
+                            amps[base + p.off[c]] = make_uint4(w[0], w[1], w[2], w[3]);
+                        }
                     }
                 }
-            }
+            };
+            if (__all_sync(0xffffffffu, (int)E >= p.fastE || !valid)) drain_tile(std::true_type{});
+            else drain_tile(std::false_type{});
             tc::fence_before_sync();
             tc::mbar_arrive(&accFree[b]);
         }
@@ -927,10 +970,11 @@ static double real_form(const double* g, int D, int n, int kk) {
 }
 
 template <int KT>
-static void prepare_ozaki_b(const double* g, std::vector<unsigned char>& bytes, int* colExp) {
+static void prepare_ozaki_b(const double* g, std::vector<unsigned char>& bytes, int* colExp, int* fastE) {
     using S = Dense<KT>;
     constexpr int D = S::D, R = S::R;
     bytes.assign(kOzBCopies * kOzSlices * S::B16, 0);
+    int minF = 1 << 20;  // over the rows with a nonzero entry (the others give zeros)
     for (int n = 0; n < R; n++) {
         int F = 0;
         bool any = false;
@@ -944,6 +988,7 @@ static void prepare_ozaki_b(const double* g, std::vector<unsigned char>& bytes, 
             }
         }
         colExp[n] = F;
+        if (any) minF = std::min(minF, F);
         for (int kk = 0; kk < R; kk++) {
             double v = real_form(g, D, n, kk);
             double scaled = std::ldexp(std::fabs(v), 48 - F);  // < 2^48, exact
@@ -961,6 +1006,8 @@ static void prepare_ozaki_b(const double* g, std::vector<unsigned char>& bytes, 
                 }
         }
     }
+    // encode_normal needs ebias = E + F_n - 141 >= -86 for every nonzero row
+    *fastE = 55 - minF;
 }
 
 // the six-target complex128 gate: 47-bit magnitudes in the digits of k_dense_ozaki6 (a
@@ -1089,7 +1136,7 @@ static int dense_tc_run(State* s, const unsigned* targs, const double* g) {
         smem = 2 * S::A32 + 2 * S::B32;
         ctasPerSM = (int)std::min<uint32_t>(4, 512 / S::COLS32);
     } else if constexpr (S::kOzakiFits) {
-        prepare_ozaki_b<KT>(g, bytes, p.colExp);
+        prepare_ozaki_b<KT>(g, bytes, p.colExp, &p.fastE);
         smem = kOzSlices * S::A16 + kOzBCopies * kOzSlices * S::B16;
         ctasPerSM = (int)(512 / S::COLS64);
     } else {

@@ -245,3 +245,29 @@ def test_dense_gate_extreme_magnitudes(dfs, oracle, prec, k, rng):
     assert rel_err(got, a) <= TOL[prec]
     zero_groups = np.abs(a) == 0
     assert np.all(got[zero_groups] == 0)
+
+
+@pytest.mark.parametrize("k", [3, 4, 5])
+@pytest.mark.parametrize("mixed", [False, True])
+def test_dense_gate_near_underflow(dfs, oracle, k, mixed, rng):
+    """Groups of amplitudes near 1e-295 (results still normal doubles): the complex128
+    tensor-core kernels encode such groups' results through their general path, which a
+    warp takes as soon as one of its groups needs it.  Either the whole state is that
+    small, or every other group (index bit 0 set, never a target) is, so that each warp
+    mixes both kinds; each kind is checked against its own largest amplitude."""
+    n = 11
+    N = 1 << n
+    a = gaussian_state(rng, N)
+    small = (np.arange(N) & 1) == 1 if mixed else np.ones(N, dtype=bool)
+    a[small] *= 1e-295
+    targs = [int(q) for q in 1 + rng.permutation(n - 1)[:k]]
+    g = gaussian_matrix(rng, 1 << k)
+    psi = dfs.StateVector(n, precision="c128")
+    psi.setAmps(a)
+    dfs.distributed_statevector_manyTargGate(psi, targs, g)
+    oracle.sv_many_targ(a, targs, g)
+    got = psi.getAllVecAmps()
+    assert np.all(np.isfinite(got))
+    assert rel_err(got[small], a[small]) <= TOL["c128"]
+    if mixed:
+        assert rel_err(got[~small], a[~small]) <= TOL["c128"]
