@@ -270,45 +270,57 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
         //      D_1 2^-8 and D_2 2^-16 exactly (TwoSum), the rest into the error term
         // in chunks of 8 output reals (4 amplitudes) so that large D stays in registers
         const uint32_t lane = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(half * D);
+        const uint32_t rowc = (uint32_t)((int)E + 896 - kOzShift) << 20;
+        // a warp whose results are all normal doubles skips the general encoding's checks
+        auto drain_tile = [&](auto normalTag) {
+            constexpr bool kNormal = decltype(normalTag)::value;
 #pragma unroll
-        for (int ch = 0; ch < D / 8; ch++) {
-            float acc[kOzAccs][8];
+            for (int ch = 0; ch < D / 8; ch++) {
+                float acc[kOzAccs][8];
 #pragma unroll
-            for (int u = 0; u < kOzAccs; u++) {
-                float v[16];
-                tc::ld8(lane + (uint32_t)(u * R + ch * 8), v);
+                for (int u = 0; u < kOzAccs; u++) {
+                    float v[16];
+                    tc::ld8(lane + (uint32_t)(u * R + ch * 8), v);
 #pragma unroll
-                for (int j = 0; j < 8; j++) acc[u][j] = v[j];
-            }
-            tc::ld_wait();
-            if (valid) {
+                    for (int j = 0; j < 8; j++) acc[u][j] = v[j];
+                }
+                tc::ld_wait();
+                if (valid) {
 #pragma unroll
-                for (int c4 = 0; c4 < 4; c4++) {
-                    const int c = ch * 4 + c4;
-                    // (re, im) of the amplitude as f32x2 pairs
-                    uint64_t a[kOzAccs];
+                    for (int c4 = 0; c4 < 4; c4++) {
+                        const int c = ch * 4 + c4;
+                        // (re, im) of the amplitude as f32x2 pairs
+                        uint64_t a[kOzAccs];
 #pragma unroll
-                    for (int u = 0; u < kOzAccs; u++) a[u] = tc::pk2(acc[u][2 * c4], acc[u][2 * c4 + 1]);
-                    uint64_t t, tl, t2, t2l, y, yl;
-                    // products by powers of two are exact, so ptxas may fuse them into the
-                    // additions that follow without changing a bit
-                    tc::two_sum2(a[0], tc::mul2(a[1], tc::pk2(0x1p-8f, 0x1p-8f)), t, tl);
-                    tc::two_sum2(t, tc::mul2(a[2], tc::pk2(0x1p-16f, 0x1p-16f)), t2, t2l);
-                    uint64_t e = tc::add2(tl, t2l);
-                    e = tc::fma2(a[3], tc::pk2(0x1p-24f, 0x1p-24f), e);
-                    e = tc::fma2(a[4], tc::pk2(0x1p-32f, 0x1p-32f), e);
-                    tc::fast_two_sum2(t2, e, y, yl);
-                    df::f2 yr, yi;
-                    tc::up2(y, yr.hi, yi.hi);
-                    tc::up2(yl, yr.lo, yi.lo);
-                    // times 2^(E + e_n - kOzShift), folded into the exponent field
-                    uint32_t w[4];
-                    df::encode_words_scaled(yr, (int)E + p.colExp[half * D + 2 * c] - kOzShift, &w[1], &w[0]);
-                    df::encode_words_scaled(yi, (int)E + p.colExp[half * D + 2 * c + 1] - kOzShift, &w[3], &w[2]);
-                    amps[base + p.off[half * kHalf + c]] = make_uint4(w[0], w[1], w[2], w[3]);
+                        for (int u = 0; u < kOzAccs; u++) a[u] = tc::pk2(acc[u][2 * c4], acc[u][2 * c4 + 1]);
+                        uint64_t t, tl, t2, t2l, y, yl;
+                        // products by powers of two are exact, so ptxas may fuse them into the
+                        // additions that follow without changing a bit
+                        tc::two_sum2(a[0], tc::mul2(a[1], tc::pk2(0x1p-8f, 0x1p-8f)), t, tl);
+                        tc::two_sum2(t, tc::mul2(a[2], tc::pk2(0x1p-16f, 0x1p-16f)), t2, t2l);
+                        uint64_t e = tc::add2(tl, t2l);
+                        e = tc::fma2(a[3], tc::pk2(0x1p-24f, 0x1p-24f), e);
+                        e = tc::fma2(a[4], tc::pk2(0x1p-32f, 0x1p-32f), e);
+                        tc::fast_two_sum2(t2, e, y, yl);
+                        df::f2 yr, yi;
+                        tc::up2(y, yr.hi, yi.hi);
+                        tc::up2(yl, yr.lo, yi.lo);
+                        // times 2^(E + e_n - kOzShift), folded into the exponent field
+                        uint32_t w[4];
+                        if constexpr (kNormal) {
+                            encode_normal(yr.hi, yr.lo, rowc + ((uint32_t)p.colExp[half * D + 2 * c] << 20), w[1], w[0]);
+                            encode_normal(yi.hi, yi.lo, rowc + ((uint32_t)p.colExp[half * D + 2 * c + 1] << 20), w[3], w[2]);
+                        } else {
+                            df::encode_words_scaled(yr, (int)E + p.colExp[half * D + 2 * c] - kOzShift, &w[1], &w[0]);
+                            df::encode_words_scaled(yi, (int)E + p.colExp[half * D + 2 * c + 1] - kOzShift, &w[3], &w[2]);
+                        }
+                        amps[base + p.off[half * kHalf + c]] = make_uint4(w[0], w[1], w[2], w[3]);
+                    }
                 }
             }
-        }
+        };
+        if (__all_sync(0xffffffffu, (int)E >= p.fastE || !valid)) drain_tile(std::true_type{});
+        else drain_tile(std::false_type{});
 #pragma unroll
         for (int c = 0; c < kHalf; c++) cur[c] = nxt[c];
     }
