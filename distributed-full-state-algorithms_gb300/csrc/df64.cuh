@@ -186,6 +186,29 @@ DF_HD void encode_words_scaled(f2 v, int shift, uint32_t* H, uint32_t* L) {
     *L = tiny ? 0u : Lr;
 }
 
+// encode_words_scaled for a result that is zero or a normal double: the caller
+// guarantees that a nonzero hi is at least 2^-75 and that hi's exponent field plus
+// ebias (= 896 + shift, passed as ebias20 = ebias << 20 modulo 2^32) is at least 1.
+// The same bits as encode_words_scaled there, without its tiny/subnormal checks.
+DF_HD void encode_words_normal(f2 v, uint32_t ebias20, uint32_t* H, uint32_t* L) {
+    uint32_t hb = fbits(v.hi);
+    uint32_t Hh = ((hb & 0x7FFFFFFFu) >> 3) + ebias20;
+    uint32_t Lh = hb << 29;
+    uint32_t sb = (306u << 23) - (hb & 0xFF800000u);
+    float scaled = mul_rn(v.lo, bitsf(sb));
+#ifdef __CUDA_ARCH__
+    int32_t off = __float2int_rn(scaled);
+#else
+    int32_t off = (int32_t)__builtin_lrintf(scaled);
+#endif
+    int32_t extra = ((hb & 0x007FFFFFu) == 0u) ? (off < 0 ? off : 0) : 0;
+    off += extra;
+    uint64_t bits = ((((uint64_t)Hh) << 32) | Lh) + (uint64_t)(int64_t)off;
+    bool zero = v.hi == 0.0f;
+    *H = zero ? (hb & 0x80000000u) : ((uint32_t)(bits >> 32) | (hb & 0x80000000u));
+    *L = zero ? 0u : (uint32_t)bits;
+}
+
 // split a double constant (host side, exact long-double free): hi = RN_float(x),
 // lo = RN_float(x - hi); |x - (hi+lo)| <= 2^-48 |x|.
 DF_HD f2 split_const(double x) {

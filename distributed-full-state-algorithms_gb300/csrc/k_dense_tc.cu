@@ -129,25 +129,11 @@ DEV uint32_t digits_dropped_below(uint32_t E32) { return (uint32_t)max((int)E32 
 // b_t 2^(40 - 8t) = g 2^(48 - F_n), so y = 2^(E + F_n - 1037) sum_u D_u 2^(-8u)
 constexpr int kOzShift = 1037;
 
-// Output y = hi + lo (a double-float with |lo| <= ulp(hi) / 2) as the double y 2^(ebias -
-// 896), rowcol = ebias << 20, for the sums of the accumulators: hi is zero or a multiple of
-// 2^-40 (every accumulator holds multiples of 2^-8, the lowest weight is 2^-32), so its
-// exponent field is >= 87 and the double is normal whenever ebias >= -86, which the host
-// guarantees through DenseParams::fastE.  As df::encode_words_scaled without the checks
-// for tiny and subnormal results: hi's bits give the high 24 bits, lo rounded to units of
-// the double's last place is added as an integer (twice when hi is a power of two and lo
-// negative, where the unit halves).
-DEV void encode_normal(float hi, float lo, uint32_t rowcol, uint32_t& Hw, uint32_t& Lw) {
-    const uint32_t hb = __float_as_uint(hi);
-    const uint32_t Hh = ((hb & 0x7FFFFFFFu) >> 3) + rowcol;
-    const uint32_t Lh = hb << 29;
-    const uint32_t sb = (306u << 23) - (hb & 0xFF800000u);  // +-2^(52 - e_hi) with hi's sign folded in
-    int32_t off = __float2int_rn(lo * __uint_as_float(sb));
-    if ((hb << 9) == 0u && off < 0) off += off;
-    const uint64_t bits = ((((uint64_t)Hh) << 32) | Lh) + (uint64_t)(int64_t)off;
-    Hw = hi == 0.f ? (hb & 0x80000000u) : ((uint32_t)(bits >> 32) | (hb & 0x80000000u));
-    Lw = hi == 0.f ? 0u : (uint32_t)bits;
-}
+// The accumulators hold multiples of 2^-8 and the lowest weight is 2^-32, so a nonzero
+// double-float sum y = hi + lo has hi >= 2^-40 (exponent field >= 87), and its double
+// y 2^(E + F_n - kOzShift) is normal whenever ebias = E + F_n - 141 >= -86, which the
+// host turns into the per-launch bound DenseParams::fastE: a warp whose groups all meet
+// it encodes with df::encode_words_normal (no tiny/subnormal checks).
 
 // the bf16 halves of two floats packed as (lo, hi)
 DEV uint32_t pack_bf16(float lo, float hi) { return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632u); }
@@ -308,8 +294,8 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
                         // times 2^(E + e_n - kOzShift), folded into the exponent field
                         uint32_t w[4];
                         if constexpr (kNormal) {
-                            encode_normal(yr.hi, yr.lo, rowc + ((uint32_t)p.colExp[half * D + 2 * c] << 20), w[1], w[0]);
-                            encode_normal(yi.hi, yi.lo, rowc + ((uint32_t)p.colExp[half * D + 2 * c + 1] << 20), w[3], w[2]);
+                            df::encode_words_normal(yr, rowc + ((uint32_t)p.colExp[half * D + 2 * c] << 20), &w[1], &w[0]);
+                            df::encode_words_normal(yi, rowc + ((uint32_t)p.colExp[half * D + 2 * c + 1] << 20), &w[3], &w[2]);
                         } else {
                             df::encode_words_scaled(yr, (int)E + p.colExp[half * D + 2 * c] - kOzShift, &w[1], &w[0]);
                             df::encode_words_scaled(yi, (int)E + p.colExp[half * D + 2 * c + 1] - kOzShift, &w[3], &w[2]);
@@ -496,8 +482,8 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
                             tc::up2(yl, yr.lo, yi.lo);
                             uint32_t w[4];
                             if constexpr (kNormal) {
-                                encode_normal(yr.hi, yr.lo, rowc + ((uint32_t)p.colExp[2 * c] << 20), w[1], w[0]);
-                                encode_normal(yi.hi, yi.lo, rowc + ((uint32_t)p.colExp[2 * c + 1] << 20), w[3], w[2]);
+                                df::encode_words_normal(yr, rowc + ((uint32_t)p.colExp[2 * c] << 20), &w[1], &w[0]);
+                                df::encode_words_normal(yi, rowc + ((uint32_t)p.colExp[2 * c + 1] << 20), &w[3], &w[2]);
                             } else {
                                 df::encode_words_scaled(yr, (int)E + p.colExp[2 * c] - kOzShift, &w[1], &w[0]);
                                 df::encode_words_scaled(yi, (int)E + p.colExp[2 * c + 1] - kOzShift, &w[3], &w[2]);
@@ -1018,7 +1004,7 @@ static void prepare_ozaki_b(const double* g, std::vector<unsigned char>& bytes, 
                 }
         }
     }
-    // encode_normal needs ebias = E + F_n - 141 >= -86 for every nonzero row
+    // df::encode_words_normal needs ebias = E + F_n - 141 >= -86 for every nonzero row
     *fastE = 55 - minF;
 }
 

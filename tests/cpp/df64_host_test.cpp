@@ -3,6 +3,7 @@
 // and the Dot2-style accumulation, against __float128 arithmetic.
 #include "../../distributed-full-state-algorithms_gb300/csrc/df64.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -90,8 +91,31 @@ int main() {
         if (std::fabs(want) < 0x1p-1020) want = 0.0;  // flushed below the normal range
         if (from_words(H2, L2) != want) scaledBad++;
     }
-    printf("decode %.3e encode %.3e dot4 %.3e zero %ld scaled %ld\n", worstDec, worstEnc, worstDot, zeroFail, scaledBad);
+    // encode_words_normal == encode_words_scaled bit for bit inside its precondition (a
+    // nonzero hi >= 2^-75, hi's exponent field + 896 + shift >= 1): the dense kernels'
+    // sums (hi a multiple of 2^-40, powers of two included, lo of either sign) and zeros
+    long normalBad = 0;
+    std::uniform_int_distribution<int> ui(0, 1 << 23);
+    for (long it = 0; it < 2000000; it++) {
+        const int e = (int)(rng() % 64) - 40;  // hi in [2^-40, 2^24)
+        float hi = std::ldexp(1.0f + (float)ui(rng) * 0x1p-23f, e);
+        if (it % 4 == 0) hi = std::ldexp(1.0f, e);
+        if (it & 1) hi = -hi;
+        float ulp = std::ldexp(1.0f, e - 23);
+        float lo = (float)(std::uniform_real_distribution<double>(-0.5, 0.5)(rng) * ulp);
+        if (it % 50 == 0) hi = lo = (it & 2) ? -0.0f : 0.0f;
+        f2 q = fast_two_sum(hi, lo);
+        const int fe = (int)((fbits(q.hi) >> 23) & 0xFF);
+        const int lowest = q.hi == 0.0f ? -1000 : 1 - fe - 896;   // smallest shift allowed
+        const int shift = std::max(lowest, (int)(rng() % 1200) - 1000);
+        uint32_t H, L, H2, L2;
+        encode_words_scaled(q, shift, &H, &L);
+        encode_words_normal(q, (uint32_t)(896 + shift) << 20, &H2, &L2);
+        if (H != H2 || L != L2) normalBad++;
+    }
+    printf("decode %.3e encode %.3e dot4 %.3e zero %ld scaled %ld normal %ld\n", worstDec, worstEnc, worstDot, zeroFail,
+           scaledBad, normalBad);
     bool ok = worstDec <= std::ldexp(1.0, -47) && worstEnc <= std::ldexp(1.0, -52) && worstDot <= std::ldexp(1.0, -44) &&
-              zeroFail == 0 && scaledBad == 0;
+              zeroFail == 0 && scaledBad == 0 && normalBad == 0;
     return ok ? 0 : 1;
 }
