@@ -247,6 +247,31 @@ def test_dense_gate_extreme_magnitudes(dfs, oracle, prec, k, rng):
     assert np.all(got[zero_groups] == 0)
 
 
+@pytest.mark.parametrize("prec", PRECISIONS)
+@pytest.mark.parametrize("k", [3, 4, 5, 6])
+@pytest.mark.parametrize("zero", ["rows", "all"])
+def test_dense_gate_zero_rows(dfs, oracle, prec, k, zero, rng):
+    """Gates with all-zero rows (whose outputs are exact zeros, and which the complex128
+    tensor-core kernels leave out of their per-row scaling bounds), and the zero gate."""
+    n = 11
+    a = gaussian_state(rng, 1 << n)
+    targs = [int(q) for q in rng.permutation(n)[:k]]
+    g = gaussian_matrix(rng, 1 << k)
+    if zero == "all":
+        g[:] = 0.0
+    else:
+        g[[0, 3], :] = 0.0
+    psi = dfs.StateVector(n, precision=prec)
+    psi.setAmps(a)
+    if prec == "c64":
+        a = psi.getAllVecAmps()
+    dfs.distributed_statevector_manyTargGate(psi, targs, g)
+    oracle.sv_many_targ(a, targs, g)
+    got = psi.getAllVecAmps()
+    assert rel_err(got, a) <= TOL[prec] or np.max(np.abs(a)) == 0
+    assert np.all(got[a == 0] == 0)
+
+
 @pytest.mark.parametrize("k", [3, 4, 5])
 @pytest.mark.parametrize("mixed", [False, True])
 def test_dense_gate_near_underflow(dfs, oracle, k, mixed, rng):
