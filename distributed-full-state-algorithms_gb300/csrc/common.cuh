@@ -150,23 +150,23 @@ struct PolF32 {  // complex64 storage and FP32 arithmetic
 };
 
 // exact unit-modulus factors applied to a value in any policy
-template <class P>
-DEV typename P::V neg(typename P::V x) {
-    typename P::V r;
-    r.re = x.re; r.im = x.im;
-    if constexpr (P::kEmulated) {
-        r.re = df::neg(x.re); r.im = df::neg(x.im);
-    } else {
-        r.re = -x.re; r.im = -x.im;
-    }
-    return r;
+// x with its sign bit xor-ed with bit 31 of m (an exact negation when it is set)
+DEV float sign_flip(float x, uint32_t m) { return __uint_as_float(__float_as_uint(x) ^ m); }
+DEV double sign_flip(double x, uint32_t m) {
+    return __longlong_as_double(__double_as_longlong(x) ^ (long long)((uint64_t)m << 32));
 }
-// multiply by i^k (k mod 4) and by (-1)^s: a re/im swap plus sign flips
+DEV df::f2 sign_flip(df::f2 x, uint32_t m) { return {sign_flip(x.hi, m), sign_flip(x.lo, m)}; }
+
+// multiply by i^k (k mod 4) and by (-1)^s: a re/im select and two sign-bit xors.  Written
+// without branches: the branching form cost the streaming sweeps that use it 5-17% at 30
+// qubits (the complex128 Pauli tensor 6.23 -> 5.14 ms).
 template <class P>
 DEV typename P::V rot(typename P::V x, int k, int s) {
-    typename P::V r = x;
-    if (k & 1) { r.re = x.im; r.im = x.re; if constexpr (P::kEmulated) r.re = df::neg(r.re); else r.re = -r.re; }
-    if ((k >> 1) ^ s) r = neg<P>(r);
+    const bool odd = k & 1;
+    const uint32_t mIm = (uint32_t)(((k >> 1) ^ s) & 1) << 31, mRe = mIm ^ ((uint32_t)odd << 31);
+    typename P::V r;
+    r.re = sign_flip(odd ? x.im : x.re, mRe);
+    r.im = sign_flip(odd ? x.re : x.im, mIm);
     return r;
 }
 

@@ -132,19 +132,28 @@ int sv_swap(State* s, unsigned q1, unsigned q2) { return dispatch<RunSwap>(s, s,
 template <class P, class IT>
 struct PauliGadgetOp {
     typename P::R c, sn;
+    typename P::K kp, kn;  // sn i^powY and its negation
     IT maskX, maskYZ;
     int top;   // highest X/Y qubit: pairs (j, j ^ X) with this bit 0
     int powY;  // #Y mod 4, plus one for the factor i of the gadget
+    int pX;    // parity(X & YZ): the sign parity of j ^ X is that of j, xor pX
     DEV void index(IT j, IT& i0, IT& i1) const {
         i0 = insert_zero(j, top);
         i1 = i0 ^ maskX;
     }
-    DEV void apply(IT i0, IT i1, typename P::V& x0, typename P::V& x1) const {
-        int s0 = parity(i0 & maskYZ), s1 = parity(i1 & maskYZ);
+    DEV void apply(IT i0, IT, typename P::V& x0, typename P::V& x1) const {
+        const int s0 = parity(i0 & maskYZ), s1 = s0 ^ pX;
         typename P::A a0 = P::first_r(c, x0);
-        P::mac_r(a0, sn, rot<P>(x1, powY, s1));
         typename P::A a1 = P::first_r(c, x1);
-        P::mac_r(a1, sn, rot<P>(x0, powY, s0));
+        if constexpr (P::kEmulated) {
+            // the partner times the complex constant +-sn i^powY: measured 5% faster at 30
+            // qubits (5.44 against 5.74 ms) than the real sn times the rotated partner
+            P::mac(a0, s1 ? kn : kp, x1);
+            P::mac(a1, s0 ? kn : kp, x0);
+        } else {  // native FP64: two fewer FP64 FMAs per amplitude the other way
+            P::mac_r(a0, sn, rot<P>(x1, powY, s1));
+            P::mac_r(a1, sn, rot<P>(x0, powY, s0));
+        }
         x0 = P::get(a0);
         x1 = P::get(a1);
     }
@@ -181,7 +190,13 @@ template <class IT>
 struct DiagSignOp {
     IT mask;
     template <class S>
-    DEV S apply_raw(IT j, S x) const { return parity(j & mask) ? raw_neg(x) : x; }
+    DEV S apply_raw(IT j, S x) const {
+        const uint32_t m = (uint32_t)parity(j & mask) << 31;
+        S r;
+        r.x = sign_flip(x.x, m);
+        r.y = sign_flip(x.y, m);
+        return r;
+    }
 };
 
 struct RunPauli {
@@ -225,6 +240,11 @@ struct RunPauli {
         op.maskYZ = (IT)mYZ;
         op.top = top;
         op.powY = (numY + 1) & 3;
+        op.pX = __builtin_parityll(mX & mYZ);
+        const double sn = std::sin(theta);
+        const double kre[4] = {sn, 0.0, -sn, 0.0}, kim[4] = {0.0, sn, 0.0, -sn};  // sn i^k
+        op.kp = P::mk(kre[op.powY], kim[op.powY]);
+        op.kn = P::mk(-kre[op.powY], -kim[op.powY]);
         return launch(k_pair<P, IT, PauliGadgetOp<P, IT>>, items, pair_per<P>(), "pauliGadget", (typename P::store*)s->amps,
                       items, op);
     }

@@ -31,15 +31,15 @@ DEV float2 raw_neg(float2 v) {
     return make_float2(__uint_as_float(__float_as_uint(v.x) ^ 0x80000000u),
                        __uint_as_float(__float_as_uint(v.y) ^ 0x80000000u));
 }
-DEV double raw_negs(double x) { return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull); }
-DEV float raw_negs(float x) { return __uint_as_float(__float_as_uint(x) ^ 0x80000000u); }
 
-// v * i^k * (-1)^s
+// v * i^k * (-1)^s, branch-free as rot (common.cuh)
 template <class S>
 DEV S raw_rot(S v, int k, int s) {
-    S r = v;
-    if (k & 1) { r.x = raw_negs(v.y); r.y = v.x; }
-    if (((k >> 1) ^ s) & 1) r = raw_neg(r);
+    const bool odd = k & 1;
+    const uint32_t mIm = (uint32_t)(((k >> 1) ^ s) & 1) << 31, mRe = mIm ^ ((uint32_t)odd << 31);
+    S r;
+    r.x = sign_flip(odd ? v.y : v.x, mRe);
+    r.y = sign_flip(odd ? v.x : v.y, mIm);
     return r;
 }
 

@@ -14,15 +14,7 @@ namespace dfs {
 // exact sign flips and multiplications by i^k of a decoded complex128 value (the
 // raw-storage forms of kernels.cuh, for amplitudes held decoded in shared memory)
 DEV PolDF::V raw_neg(PolDF::V v) { return {df::neg(v.re), df::neg(v.im)}; }
-DEV PolDF::V raw_rot(PolDF::V v, int k, int s) {
-    PolDF::V r = v;
-    if (k & 1) {
-        r.re = df::neg(v.im);
-        r.im = v.re;
-    }
-    if (((k >> 1) ^ s) & 1) r = raw_neg(r);
-    return r;
-}
+DEV PolDF::V raw_rot(PolDF::V v, int k, int s) { return rot<PolDF>(v, k, s); }
 
 namespace batch {
 
