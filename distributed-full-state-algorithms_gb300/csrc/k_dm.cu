@@ -46,11 +46,11 @@ int dm_deph1(State* s, unsigned q, double p) { return dispatch<RunDeph1>(s, s, q
 // scale by 1 - 4p/3 where the ket and bra bits of qb1 or of qb2 differ.
 template <class P, class IT>
 struct Deph2Op {
-    typename P::R f;
+    typename P::R f, one;
     int q1, q1a, q2, q2a;
     DEV typename P::V apply(IT j, typename P::V x) const {
         IT d = ((j >> q1) ^ (j >> q1a)) | ((j >> q2) ^ (j >> q2a));
-        return (d & 1) ? P::scale(f, x) : x;
+        return P::scale((d & 1) ? f : one, x);  // no branch; a product by one is exact
     }
 };
 
@@ -58,7 +58,7 @@ struct RunDeph2 {
     template <class P, class IT>
     static int run(State* s, unsigned q1, unsigned q2, double p) {
         unsigned n = s->numQubits;
-        Deph2Op<P, IT> op{P::mkr(1 - 4 * p / 3), (int)q1, (int)(q1 + n), (int)q2, (int)(q2 + n)};
+        Deph2Op<P, IT> op{P::mkr(1 - 4 * p / 3), P::mkr(1.0), (int)q1, (int)(q1 + n), (int)q2, (int)(q2 + n)};
         IT items = (IT)s->numAmps;
         return launch(k_diag<P, IT, Deph2Op<P, IT>>, items, diag_per<P>(), "twoQubitDephasing", (typename P::store*)s->amps,
                       items, op);
