@@ -88,6 +88,7 @@ PROTOTYPES = {
     "dfs_state_set_zero": [_H],
     "dfs_state_set_classical": [_H, _U64],
     "dfs_state_set_random": [_H, _U64, _I],
+    "dfs_state_magnitude": [_H, _DP, _DP, C.POINTER(_I)],
     "dfs_wait_selftest": [_D, _U, C.POINTER(_I), C.POINTER(_I)],
     "dfs_state_save": [_H, C.c_char_p],
     "dfs_state_load": [C.c_char_p, _HP],
@@ -112,6 +113,7 @@ PROTOTYPES = {
     "dfs_densitymatrix_damping": [_H, _U, _D],
     "dfs_densitymatrix_expecPauliString": [_H, _DP, _U, _UP, _DP, _DP],
     "dfs_densitymatrix_partialTrace": [_H, _UP, _U, _HP],
+    "dfs_densitymatrix_partialTrace_into": [_H, _UP, _U, _H],
     "dfs_statevector_expecPauliSum": [_H, _DP, _U, _UP, _DP, _DP],
     "dfs_state_inner_product": [_H, _H, _DP, _DP],
     "dfs_state_norm_squared": [_H, _DP],

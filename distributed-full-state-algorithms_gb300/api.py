@@ -156,6 +156,15 @@ class StateVector:
     def copyFrom(self, other: "StateVector") -> None:
         call("dfs_state_copy", self._h, other._h)
 
+    def magnitude(self) -> dict:
+        """The engine's log2 bounds on the amplitude vector's 2-norm (complex128 states)
+        and whether the next operation takes the native FP64 arithmetic
+        (``dfs_state_magnitude``)."""
+        hi, lo, fl = C.c_double(), C.c_double(), C.c_int()
+        call("dfs_state_magnitude", self._h, C.byref(hi), C.byref(lo), C.byref(fl))
+        return {"log2_norm_hi": hi.value, "log2_norm_lo": lo.value, "non_finite": bool(fl.value & 1),
+                "native": bool(fl.value & 2)}
+
     def device_ptr(self) -> int:
         p = C.c_void_p()
         call("dfs_state_device_ptr", self._h, C.byref(p))
@@ -382,9 +391,14 @@ def distributed_densitymatrix_expecPauliString(rho: DensityMatrix, coeffs, allPa
     return complex(re.value, im.value)
 
 
-def distributed_densitymatrix_partialTrace(rho: DensityMatrix, targets) -> DensityMatrix:
+def distributed_densitymatrix_partialTrace(rho: DensityMatrix, targets, out: DensityMatrix | None = None) -> DensityMatrix:
+    """The reduced density matrix (a new one, or written into ``out``)."""
     _dm_check(rho)
     t, k = _uarr(targets)
+    if out is not None:
+        _dm_check(out)
+        call("dfs_densitymatrix_partialTrace_into", rho.handle, t, k, out.handle)
+        return out
     h = C.c_void_p()
     call("dfs_densitymatrix_partialTrace", rho.handle, t, k, C.byref(h))
     return DensityMatrix(0, _handle=h)

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
 #include <mutex>
 #include <new>
 #include <vector>
@@ -157,7 +158,7 @@ static int check_paulis(const unsigned* p, unsigned num) {
     return DFS_SUCCESS;
 }
 
-static int new_state(unsigned n, int isDM, int precision, dfs_state* out) {
+static int new_state(unsigned n, int isDM, int precision, dfs_state* out, bool zeroFill = true) {
     int rc = ensure_init();
     if (rc) return rc;
     if (!out) return fail(DFS_ERR_INVALID_ARG, "null output handle");
@@ -179,7 +180,7 @@ static int new_state(unsigned n, int isDM, int precision, dfs_state* out) {
         delete s;
         return cuda_fail(e, "state allocation");
     }
-    e = cudaMemsetAsync(s->amps, 0, bytes, g_ctx.stream);
+    if (zeroFill) e = cudaMemsetAsync(s->amps, 0, bytes, g_ctx.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g_ctx.stream);
     if (e != cudaSuccess) {
         cudaFree(s->amps);
@@ -196,10 +197,38 @@ static std::vector<unsigned> shifted(const unsigned* t, unsigned k, unsigned by)
     return v;
 }
 
-static bool odd_num_y(const unsigned* p, unsigned k) {
-    int c = 0;
-    for (unsigned i = 0; i < k; i++) c += p[i] == 2;
-    return c & 1;
+// runs one operation under the range guard (range.cu): the arithmetic is chosen from
+// the state's magnitude bounds and the operation's, and the bounds follow the operation
+template <class F>
+static int guarded(State* s, const OpBound& b, F&& f) {
+    int rc = range_select(s, b);
+    if (rc) return rc;
+    rc = f();
+    range_after(s, b, rc);
+    return rc;
+}
+
+// a reduction over s (and t) under the range guard; the state is unchanged
+template <class F>
+static int guarded_reduce(State* s, State* t, double lgSum, bool quadratic, F&& f) {
+    int rc = range_select_reduce(s, t, lgSum, quadratic);
+    if (rc) return rc;
+    rc = f();
+    s->forceNative = false;
+    return rc;
+}
+
+static OpBound bound_angle(double theta) {
+    OpBound b;
+    b.finite = std::isfinite(theta);
+    return b;
+}
+
+// U on the ket qubits and conj(U) on the bra qubits: singular values multiply
+static OpBound bound_dm_unitary(OpBound u) {
+    u.grow *= 2;
+    u.shrink *= 2;
+    return u;
 }
 
 }  // namespace dfs
@@ -288,6 +317,7 @@ int dfs_state_destroy(dfs_state s) {
         cudaEventSynchronize(s->copyDone);
         cudaEventDestroy(s->copyDone);
     }
+    range_release(s);
     cudaFree(s->amps);
     delete s;
     return DFS_SUCCESS;
@@ -315,6 +345,9 @@ int dfs_state_device_ptr(dfs_state s, void** ptr) {
         s->copyPending = false;
     }
     *ptr = s->amps;
+    // the caller may write through the pointer: magnitudes are re-measured before the
+    // next operation
+    range_forget(s);
     return DFS_SUCCESS;
 }
 
@@ -331,7 +364,9 @@ static int check_range(dfs_state s, const void* p, uint64_t start, uint64_t coun
 int dfs_state_set_amps(dfs_state s, const double* amps, uint64_t start, uint64_t count) {
     DFS_TRACE_CALL();
     int rc = check_range(s, amps, start, count);
-    return rc ? rc : (count ? state_upload(s, amps, start, count) : DFS_SUCCESS);
+    if (rc || !count) return rc;
+    range_forget(s);
+    return state_upload(s, amps, start, count);
 }
 
 int dfs_state_get_amps(dfs_state s, double* amps, uint64_t start, uint64_t count) {
@@ -345,6 +380,7 @@ int dfs_state_set_raw(dfs_state s, const void* src, uint64_t start, uint64_t cou
     int rc = check_range(s, src, start, count);
     if (rc || !count) return rc;
     size_t eb = elem_bytes(s->precision);
+    range_forget(s);
     cudaError_t e =
         cudaMemcpyAsync((char*)s->amps + start * eb, src, count * eb, cudaMemcpyHostToDevice, g_ctx.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g_ctx.stream);
@@ -381,7 +417,14 @@ static int transfer_async(dfs_state s, void* host, uint64_t start, uint64_t coun
     if (e == cudaSuccess)
         e = toDevice ? cudaMemcpyAsync(dev, host, count * eb, cudaMemcpyHostToDevice, g_ctx.copyStream)
                      : cudaMemcpyAsync(host, dev, count * eb, cudaMemcpyDeviceToHost, g_ctx.copyStream);
-    if (e == cudaSuccess) e = cudaEventRecord(s->copyDone, g_ctx.copyStream);
+    if (e != cudaSuccess) return cuda_fail(e, "asynchronous state transfer");
+    // new content: its magnitudes are measured right behind the copy, on the copy stream,
+    // and read back by the first operation that needs them
+    if (toDevice) {
+        int rc2 = range_measure_async(s, g_ctx.copyStream);
+        if (rc2) return rc2;
+    }
+    e = cudaEventRecord(s->copyDone, g_ctx.copyStream);
     if (e != cudaSuccess) return cuda_fail(e, "asynchronous state transfer");
     s->copyPending = true;
     return DFS_SUCCESS;
@@ -413,16 +456,23 @@ int dfs_state_copy(dfs_state dst, dfs_state src) {
     if (dst->numAmps != src->numAmps || dst->isDM != src->isDM || dst->numQubits != src->numQubits)
         return fail(DFS_ERR_INVALID_ARG, "states differ in shape");
     if (dst == src) return DFS_SUCCESS;
-    if (elem_bytes(dst->precision) != elem_bytes(src->precision)) return state_convert(dst, src);
+    if (elem_bytes(dst->precision) != elem_bytes(src->precision)) {
+        range_forget(dst);
+        return state_convert(dst, src);
+    }
+    range_copy(dst, src);
     cudaError_t e = cudaMemcpyAsync(dst->amps, src->amps, src->numAmps * elem_bytes(src->precision),
                                     cudaMemcpyDeviceToDevice, g_ctx.stream);
+    if (e != cudaSuccess) range_forget(dst);
     return e == cudaSuccess ? DFS_SUCCESS : cuda_fail(e, "state copy");
 }
 
 int dfs_state_set_zero(dfs_state s) {
     DFS_TRACE_CALL();
     int rc = check_state(s);
-    return rc ? rc : state_fill_zero(s);
+    if (rc) return rc;
+    range_set(s, -std::numeric_limits<double>::infinity());
+    return state_fill_zero(s);
 }
 
 int dfs_state_set_classical(dfs_state s, uint64_t index) {
@@ -430,13 +480,21 @@ int dfs_state_set_classical(dfs_state s, uint64_t index) {
     int rc = check_state(s);
     if (rc) return rc;
     if (index >= s->numAmps) return fail(DFS_ERR_INVALID_ARG, "index %llu out of range", (unsigned long long)index);
+    range_set(s, 0.0);
     return state_set_classical(s, index);
 }
 
 int dfs_state_set_random(dfs_state s, uint64_t seed, int normalise) {
     DFS_TRACE_CALL();
     int rc = check_state(s);
-    return rc ? rc : state_set_random(s, seed, normalise);
+    if (rc) return rc;
+    // the generator's values are normal floats below 6 in magnitude (inside the
+    // double-float window, so its own normalisation runs there); a normalised result has
+    // unit norm, an unnormalised one is measured when next needed
+    rc = state_set_random(s, seed, normalise);
+    if (!rc && normalise) range_set(s, 0.0);
+    else range_forget(s);
+    return rc;
 }
 
 // ------------------------------------------------------ statevector gates
@@ -446,7 +504,8 @@ int dfs_statevector_oneTargGate(dfs_state s, unsigned target, const double* gate
     int rc = check_state(s);
     if (!rc) rc = check_qubit(target, s->vecQubits, "target");
     if (!rc && !gate) rc = fail(DFS_ERR_INVALID_ARG, "null gate");
-    return rc ? rc : sv_one_targ(s, target, gate);
+    if (rc) return rc;
+    return guarded(s, bound_matrix(gate, 2), [&] { return sv_one_targ(s, target, gate); });
 }
 
 int dfs_statevector_manyCtrlOneTargGate(dfs_state s, const unsigned* controls, unsigned nc, unsigned target,
@@ -460,7 +519,10 @@ int dfs_statevector_manyCtrlOneTargGate(dfs_state s, const unsigned* controls, u
             if (controls[i] == target) rc = fail(DFS_ERR_DUPLICATE_QUBIT, "control %u is also the target", target);
     if (!rc && nc + 1 > s->vecQubits) rc = fail(DFS_ERR_TOO_LARGE, "too many controls");
     if (!rc && !gate) rc = fail(DFS_ERR_INVALID_ARG, "null gate");
-    return rc ? rc : sv_ctrl_one_targ(s, controls, nc, target, gate);
+    if (rc) return rc;
+    // identity where a control is 0, the gate where all are 1
+    return guarded(s, bound_join(bound_matrix(gate, 2), OpBound{}),
+                   [&] { return sv_ctrl_one_targ(s, controls, nc, target, gate); });
 }
 
 int dfs_statevector_swapGate(dfs_state s, unsigned qb1, unsigned qb2) {
@@ -469,7 +531,7 @@ int dfs_statevector_swapGate(dfs_state s, unsigned qb1, unsigned qb2) {
     if (!rc) rc = check_qubit(qb1, s->vecQubits, "qubit");
     if (!rc) rc = check_qubit(qb2, s->vecQubits, "qubit");
     if (rc) return rc;
-    return qb1 == qb2 ? DFS_SUCCESS : sv_swap(s, qb1, qb2);
+    return qb1 == qb2 ? DFS_SUCCESS : guarded(s, OpBound{}, [&] { return sv_swap(s, qb1, qb2); });
 }
 
 int dfs_statevector_manyTargGate(dfs_state s, const unsigned* targets, unsigned k, const double* gate) {
@@ -477,7 +539,8 @@ int dfs_statevector_manyTargGate(dfs_state s, const unsigned* targets, unsigned 
     int rc = check_state(s);
     if (!rc) rc = check_list(targets, k, s->vecQubits, "target", false);
     if (!rc && !gate) rc = fail(DFS_ERR_INVALID_ARG, "null gate");
-    return rc ? rc : sv_many_targ(s, targets, k, gate);
+    if (rc) return rc;
+    return guarded(s, bound_matrix(gate, (size_t)1 << k), [&] { return sv_many_targ(s, targets, k, gate); });
 }
 
 int dfs_statevector_pauliTensor(dfs_state s, const unsigned* targets, const unsigned* paulis, unsigned k) {
@@ -485,7 +548,8 @@ int dfs_statevector_pauliTensor(dfs_state s, const unsigned* targets, const unsi
     int rc = check_state(s);
     if (!rc) rc = check_list(targets, k, s->vecQubits, "target", true);
     if (!rc) rc = check_paulis(paulis, k);
-    return rc ? rc : sv_pauli(s, targets, paulis, k, 0, 0.0);
+    if (rc) return rc;
+    return guarded(s, OpBound{}, [&] { return sv_pauli(s, targets, paulis, k, 0, 0.0); });
 }
 
 int dfs_statevector_pauliGadget(dfs_state s, const unsigned* targets, const unsigned* paulis, unsigned k,
@@ -494,14 +558,16 @@ int dfs_statevector_pauliGadget(dfs_state s, const unsigned* targets, const unsi
     int rc = check_state(s);
     if (!rc) rc = check_list(targets, k, s->vecQubits, "target", true);
     if (!rc) rc = check_paulis(paulis, k);
-    return rc ? rc : sv_pauli(s, targets, paulis, k, 1, theta);
+    if (rc) return rc;
+    return guarded(s, bound_angle(theta), [&] { return sv_pauli(s, targets, paulis, k, 1, theta); });
 }
 
 int dfs_statevector_phaseGadget(dfs_state s, const unsigned* targets, unsigned k, double theta) {
     DFS_TRACE_CALL();
     int rc = check_state(s);
     if (!rc) rc = check_list(targets, k, s->vecQubits, "target", true);
-    return rc ? rc : sv_phase_gadget(s, targets, k, theta);
+    if (rc) return rc;
+    return guarded(s, bound_angle(theta), [&] { return sv_phase_gadget(s, targets, k, theta); });
 }
 
 // --------------------------------------------------------- density matrix
@@ -513,6 +579,7 @@ int dfs_densitymatrix_manyTargGate(dfs_state s, const unsigned* targets, unsigne
     if (!rc && !gate) rc = fail(DFS_ERR_INVALID_ARG, "null gate");
     if (rc) return rc;
     size_t d = (size_t)1 << k;
+    const OpBound bound = bound_dm_unitary(bound_matrix(gate, d));
     if (k <= 2 && s->precision != DFS_C128_NATIVE) {
         // one sweep of the superoperator U (x) conj(U) on targets ++ targets+n (the
         // layout of getSuperoperator, src/misc.hpp:58-81): local index a + d*b with ket
@@ -528,13 +595,17 @@ int dfs_densitymatrix_manyTargGate(dfs_state s, const unsigned* targets, unsigne
                         S[(a + d * b) * sd + (ap + d * bp)] = U[a * d + ap] * std::conj(U[b * d + bp]);
         std::vector<unsigned> ext(targets, targets + k);
         for (unsigned i = 0; i < k; i++) ext.push_back(targets[i] + s->numQubits);
-        return sv_many_targ(s, ext.data(), 2 * k, reinterpret_cast<const double*>(S.data()));
+        return guarded(s, bound, [&] {
+            return sv_many_targ(s, ext.data(), 2 * k, reinterpret_cast<const double*>(S.data()));
+        });
     }
-    if ((rc = sv_many_targ(s, targets, k, gate))) return rc;
     std::vector<double> conjGate(gate, gate + 2 * d * d);
     for (size_t e = 0; e < d * d; e++) conjGate[2 * e + 1] = -conjGate[2 * e + 1];
     std::vector<unsigned> bra = shifted(targets, k, s->numQubits);
-    return sv_many_targ(s, bra.data(), k, conjGate.data());
+    return guarded(s, bound, [&] {
+        int r = sv_many_targ(s, targets, k, gate);
+        return r ? r : sv_many_targ(s, bra.data(), k, conjGate.data());
+    });
 }
 
 int dfs_densitymatrix_swapGate(dfs_state s, unsigned qb1, unsigned qb2) {
@@ -543,8 +614,8 @@ int dfs_densitymatrix_swapGate(dfs_state s, unsigned qb1, unsigned qb2) {
     if (!rc) rc = check_qubit(qb1, s->numQubits, "qubit");
     if (!rc) rc = check_qubit(qb2, s->numQubits, "qubit");
     if (rc || qb1 == qb2) return rc;
-    if ((rc = sv_swap(s, qb1, qb2))) return rc;
-    return sv_swap(s, qb1 + s->numQubits, qb2 + s->numQubits);
+    // the ket swap and the bra swap as one exact sweep (src/distributed_densitymatrix.hpp:28-33)
+    return guarded(s, OpBound{}, [&] { return dm_swap(s, qb1, qb2); });
 }
 
 int dfs_densitymatrix_pauliTensor(dfs_state s, const unsigned* targets, const unsigned* paulis, unsigned k) {
@@ -553,10 +624,7 @@ int dfs_densitymatrix_pauliTensor(dfs_state s, const unsigned* targets, const un
     if (!rc) rc = check_list(targets, k, s->numQubits, "target", true);
     if (!rc) rc = check_paulis(paulis, k);
     if (rc) return rc;
-    if ((rc = sv_pauli(s, targets, paulis, k, 0, 0.0))) return rc;
-    std::vector<unsigned> bra = shifted(targets, k, s->numQubits);
-    if ((rc = sv_pauli(s, bra.data(), paulis, k, 0, 0.0))) return rc;
-    return odd_num_y(paulis, k) ? state_scale_real(s, -1.0) : DFS_SUCCESS;
+    return guarded(s, OpBound{}, [&] { return dm_pauli_tensor(s, targets, paulis, k); });
 }
 
 int dfs_densitymatrix_pauliGadget(dfs_state s, const unsigned* targets, const unsigned* paulis, unsigned k,
@@ -566,9 +634,7 @@ int dfs_densitymatrix_pauliGadget(dfs_state s, const unsigned* targets, const un
     if (!rc) rc = check_list(targets, k, s->numQubits, "target", true);
     if (!rc) rc = check_paulis(paulis, k);
     if (rc) return rc;
-    if ((rc = sv_pauli(s, targets, paulis, k, 1, theta))) return rc;
-    std::vector<unsigned> bra = shifted(targets, k, s->numQubits);
-    return sv_pauli(s, bra.data(), paulis, k, 1, odd_num_y(paulis, k) ? theta : -theta);
+    return guarded(s, bound_angle(theta), [&] { return dm_pauli_gadget(s, targets, paulis, k, theta); });
 }
 
 int dfs_densitymatrix_phaseGadget(dfs_state s, const unsigned* targets, unsigned k, double theta) {
@@ -576,9 +642,7 @@ int dfs_densitymatrix_phaseGadget(dfs_state s, const unsigned* targets, unsigned
     int rc = check_dm(s);
     if (!rc) rc = check_list(targets, k, s->numQubits, "target", true);
     if (rc) return rc;
-    if ((rc = sv_phase_gadget(s, targets, k, theta))) return rc;
-    std::vector<unsigned> bra = shifted(targets, k, s->numQubits);
-    return sv_phase_gadget(s, bra.data(), k, -theta);
+    return guarded(s, bound_angle(theta), [&] { return dm_phase_gadget(s, targets, k, theta); });
 }
 
 int dfs_densitymatrix_krausMap(dfs_state s, const double* ops, unsigned numOps, const unsigned* targets,
@@ -603,14 +667,19 @@ int dfs_densitymatrix_krausMap(dfs_state s, const double* ops, unsigned numOps, 
     }
     std::vector<unsigned> ext(targets, targets + k);
     for (unsigned i = 0; i < k; i++) ext.push_back(targets[i] + s->numQubits);
-    return sv_many_targ(s, ext.data(), 2 * k, reinterpret_cast<const double*>(S.data()));
+    const double* Sd = reinterpret_cast<const double*>(S.data());
+    OpBound b = bound_matrix(Sd, sd);
+    for (size_t i = 0; i < 2 * (size_t)numOps * d * d; i++)
+        if (!std::isfinite(ops[i])) b.finite = false;
+    return guarded(s, b, [&] { return sv_many_targ(s, ext.data(), 2 * k, Sd); });
 }
 
 int dfs_densitymatrix_oneQubitDephasing(dfs_state s, unsigned qb, double prob) {
     DFS_TRACE_CALL();
     int rc = check_dm(s);
     if (!rc) rc = check_qubit(qb, s->numQubits, "qubit");
-    return rc ? rc : dm_deph1(s, qb, prob);
+    if (rc) return rc;
+    return guarded(s, bound_channel(CHAN_DEPH1, prob), [&] { return dm_deph1(s, qb, prob); });
 }
 
 static int check_two(dfs_state s, unsigned q1, unsigned q2) {
@@ -624,33 +693,38 @@ static int check_two(dfs_state s, unsigned q1, unsigned q2) {
 int dfs_densitymatrix_twoQubitDephasing(dfs_state s, unsigned qb1, unsigned qb2, double prob) {
     DFS_TRACE_CALL();
     int rc = check_two(s, qb1, qb2);
-    return rc ? rc : dm_deph2(s, qb1, qb2, prob);
+    if (rc) return rc;
+    return guarded(s, bound_channel(CHAN_DEPH2, prob), [&] { return dm_deph2(s, qb1, qb2, prob); });
 }
 
 int dfs_densitymatrix_oneQubitDepolarising(dfs_state s, unsigned qb, double prob) {
     DFS_TRACE_CALL();
     int rc = check_dm(s);
     if (!rc) rc = check_qubit(qb, s->numQubits, "qubit");
-    return rc ? rc : dm_depol1(s, qb, prob);
+    if (rc) return rc;
+    return guarded(s, bound_channel(CHAN_DEPOL1, prob), [&] { return dm_depol1(s, qb, prob); });
 }
 
 int dfs_densitymatrix_twoQubitDepolarising(dfs_state s, unsigned qb1, unsigned qb2, double prob) {
     DFS_TRACE_CALL();
     int rc = check_two(s, qb1, qb2);
-    return rc ? rc : dm_depol2(s, qb1, qb2, prob, 0);
+    if (rc) return rc;
+    return guarded(s, bound_channel(CHAN_DEPOL2, prob), [&] { return dm_depol2(s, qb1, qb2, prob, 0); });
 }
 
 int dfs_densitymatrix_twoQubitDepolarising_referenceCompat(dfs_state s, unsigned qb1, unsigned qb2, double prob) {
     DFS_TRACE_CALL();
     int rc = check_two(s, qb1, qb2);
-    return rc ? rc : dm_depol2(s, qb1, qb2, prob, 1);
+    if (rc) return rc;
+    return guarded(s, bound_channel(CHAN_DEPOL2_COMPAT, prob), [&] { return dm_depol2(s, qb1, qb2, prob, 1); });
 }
 
 int dfs_densitymatrix_damping(dfs_state s, unsigned qb, double prob) {
     DFS_TRACE_CALL();
     int rc = check_dm(s);
     if (!rc) rc = check_qubit(qb, s->numQubits, "qubit");
-    return rc ? rc : dm_damping(s, qb, prob);
+    if (rc) return rc;
+    return guarded(s, bound_channel(CHAN_DAMPING, prob), [&] { return dm_damping(s, qb, prob); });
 }
 
 int dfs_densitymatrix_expecPauliString(dfs_state s, const double* coeffs, unsigned numTerms,
@@ -666,7 +740,33 @@ int dfs_densitymatrix_expecPauliString(dfs_state s, const double* coeffs, unsign
         *im = 0;
         return DFS_SUCCESS;
     }
-    return dm_expec_pauli(s, coeffs, numTerms, allPaulis, re, im);
+    // The reference multiplies every element of rho by the Pauli tensor's element
+    // (src/misc.hpp:16-38, src/distributed_densitymatrix.hpp:322-344), zeros included, so a
+    // NaN or Inf anywhere in rho makes its result NaN; the engine reads only the 2^n
+    // elements a term can weight, and returns that NaN explicitly.
+    if ((rc = range_confirm_non_finite(s))) return rc;
+    if (s->precision == DFS_C128 && s->nonFinite) {
+        *re = *im = std::numeric_limits<double>::quiet_NaN();
+        return DFS_SUCCESS;
+    }
+    // a term's partial sum adds 2^n elements of the matrix: at most 2^(n/2) times its 2-norm
+    return guarded_reduce(s, nullptr, 0.5 * s->numQubits, false,
+                          [&] { return dm_expec_pauli(s, coeffs, numTerms, allPaulis, re, im); });
+}
+
+int dfs_densitymatrix_partialTrace_into(dfs_state s, const unsigned* targets, unsigned k, dfs_state out) {
+    DFS_TRACE_CALL();
+    int rc = check_dm(s);
+    if (!rc) rc = check_list(targets, k, s->numQubits, "target", true);
+    if (!rc) rc = check_dm(out);
+    if (rc) return rc;
+    if (out == s) return fail(DFS_ERR_INVALID_ARG, "the output must be another state");
+    if (out->numQubits != s->numQubits - k || out->precision != s->precision)
+        return fail(DFS_ERR_INVALID_ARG, "the output must be a %u-qubit density matrix of the input's precision",
+                    s->numQubits - k);
+    rc = guarded_reduce(s, nullptr, 0.5 * k, false, [&] { return dm_partial_trace(s, targets, k, out); });
+    range_forget(out);
+    return rc;
 }
 
 int dfs_densitymatrix_partialTrace(dfs_state s, const unsigned* targets, unsigned k, dfs_state* out) {
@@ -676,11 +776,15 @@ int dfs_densitymatrix_partialTrace(dfs_state s, const unsigned* targets, unsigne
     if (!rc && !out) rc = fail(DFS_ERR_INVALID_ARG, "null output handle");
     if (rc) return rc;
     dfs_state r = nullptr;
-    if ((rc = new_state(s->numQubits - k, 1, s->precision, &r))) return rc;
-    if ((rc = dm_partial_trace(s, targets, k, r))) {
+    // every output element is written by the kernel: no zero-fill
+    if ((rc = new_state(s->numQubits - k, 1, s->precision, &r, false))) return rc;
+    // an output element adds 2^k input elements: at most 2^(k/2) times the input's 2-norm
+    rc = guarded_reduce(s, nullptr, 0.5 * k, false, [&] { return dm_partial_trace(s, targets, k, r); });
+    if (rc) {
         dfs_state_destroy(r);
         return rc;
     }
+    range_forget(r);
     *out = r;
     return DFS_SUCCESS;
 }
@@ -700,9 +804,14 @@ int dfs_statevector_expecPauliSum(dfs_state s, const double* coeffs, unsigned nu
         *im = 0;
         return DFS_SUCCESS;
     }
+    // a term's partial sum is at most twice the squared 2-norm
+    rc = range_select_reduce(s, nullptr, 1.0, true);
+    if (rc) return rc;
     State view = *s;
     view.numQubits = s->vecQubits;  // terms address every bit of the vector
-    return sv_expec_pauli_sum(&view, coeffs, numTerms, allPaulis, re, im);
+    rc = sv_expec_pauli_sum(&view, coeffs, numTerms, allPaulis, re, im);
+    s->forceNative = false;
+    return rc;
 }
 
 int dfs_state_inner_product(dfs_state a, dfs_state b, double* re, double* im) {
@@ -713,21 +822,23 @@ int dfs_state_inner_product(dfs_state a, dfs_state b, double* re, double* im) {
     if (rc) return rc;
     if (a->numAmps != b->numAmps) return fail(DFS_ERR_INVALID_ARG, "states differ in size");
     if (a->precision != b->precision) return fail(DFS_ERR_PRECISION, "states differ in precision");
-    return state_inner(a, b, re, im);
+    return guarded_reduce(a, b, 0.0, true, [&] { return state_inner(a, b, re, im); });
 }
 
 int dfs_state_norm_squared(dfs_state s, double* out) {
     DFS_TRACE_CALL();
     int rc = check_state(s);
     if (!rc && !out) rc = fail(DFS_ERR_INVALID_ARG, "null output");
-    return rc ? rc : state_norm2(s, out);
+    if (rc) return rc;
+    return guarded_reduce(s, nullptr, 0.0, true, [&] { return state_norm2(s, out); });
 }
 
 int dfs_densitymatrix_trace(dfs_state s, double* re, double* im) {
     DFS_TRACE_CALL();
     int rc = check_dm(s);
     if (!rc && (!re || !im)) rc = fail(DFS_ERR_INVALID_ARG, "null output");
-    return rc ? rc : dm_trace(s, re, im);
+    if (rc) return rc;
+    return guarded_reduce(s, nullptr, 0.5 * s->numQubits, false, [&] { return dm_trace(s, re, im); });
 }
 
 }  // extern "C"

@@ -22,6 +22,10 @@
 
 namespace dfs {
 
+// log2 of the largest sum of |coefficients| of a complex128 batch's Hamiltonians
+constexpr double kBatchLgCoeffs = 40.0;
+
+
 struct BatchRow {
     unsigned circuit;
     int param;  // parameter index within the circuit
@@ -511,6 +515,17 @@ int dfs_batch_set_state(dfs_batch b, unsigned index, dfs_state s) {
     if (s->precision != b->precision) return fail(DFS_ERR_PRECISION, "state precision differs from the batch's");
     int rc = state_acquire(s);
     if (rc) return rc;
+    if (b->precision == DFS_C128) {
+        // the batched kernel has no native-FP64 fallback of its own: a complex128 batch takes
+        // states inside the double-float window with room for the Hamiltonian (range.cu)
+        bool native = false;
+        if ((rc = range_decide(s, OpBound{}, kBatchLgCoeffs, &native))) return rc;
+        if (native || 2.0 * s->lgHi + kBatchLgCoeffs > 118.0)
+            return fail(DFS_ERR_PRECISION,
+                        "state %u has amplitudes outside the complex128 double-float range (non-finite, or "
+                        "a 2-norm outside [2^%g, 2^%g]); a DFS_C128_NATIVE batch takes it",
+                        index, 0.5 * std::log2(2.0 * (double)s->numAmps) - 30.0, (118.0 - kBatchLgCoeffs) / 2);
+    }
     State v = arena_view(b, 0, index);
     cudaError_t e = cudaMemcpyAsync(v.amps, s->amps, v.numAmps * elem_bytes(b->precision), cudaMemcpyDeviceToDevice,
                                     ctx().stream);
@@ -538,6 +553,7 @@ int dfs_batch_get_state(dfs_batch b, unsigned index, dfs_state out) {
         return fail(DFS_ERR_STATE_KIND, "state does not match circuit %u", index);
     int rc = state_acquire(out);
     if (rc) return rc;
+    range_forget(out);
     State v = arena_view(b, 1, index);
     cudaError_t e = cudaMemcpyAsync(out->amps, v.amps, v.numAmps * elem_bytes(b->precision),
                                     cudaMemcpyDeviceToDevice, ctx().stream);
@@ -552,6 +568,14 @@ int dfs_batch_set_hamiltonian(dfs_batch b, unsigned index, const double* coeffs,
     if (index >= b->num) return fail(DFS_ERR_INVALID_ARG, "circuit %u of %u", index, b->num);
     if (numTerms == 0 || numTerms > (unsigned)batch::kMaxTerms || !coeffs || !allPaulis)
         return fail(DFS_ERR_INVALID_ARG, "a batched Hamiltonian has 1 to %d terms", batch::kMaxTerms);
+    if (b->precision == DFS_C128) {
+        long double sum = 0;
+        for (unsigned t = 0; t < numTerms; t++) sum += std::fabs(coeffs[t]);
+        if (!(sum <= std::ldexp(1.0L, (int)kBatchLgCoeffs)))
+            return fail(DFS_ERR_PRECISION,
+                        "a complex128 batch takes Hamiltonians with sum |c| up to 2^%g (double-float range); "
+                        "a DFS_C128_NATIVE batch takes any", kBatchLgCoeffs);
+    }
     const unsigned n = b->nq[index];
     std::vector<AdjTerm> ts(numTerms);
     for (unsigned t = 0; t < numTerms; t++) {

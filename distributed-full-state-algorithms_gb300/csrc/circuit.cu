@@ -696,6 +696,51 @@ static int backward(Circuit* c, const double* params, double* grad) {
     return DFS_SUCCESS;
 }
 
+// ---------------------------------------------------------- magnitude window
+// The combined 2-norm bound of a circuit's operations at these parameter values (every
+// prefix of the circuit stays inside it), for the complex128 range guard (range.cu).
+static OpBound circuit_bound(const Circuit* c, const double* params) {
+    OpBound t;
+    for (const CircOp& op : c->ops) {
+        OpBound b;
+        const double v = op.val(params);
+        switch (op.kind) {
+            case OP_ONE_TARG:
+            case OP_MANY_TARG: b = bound_matrix(op.gate.data(), (size_t)1 << op.targs.size()); break;
+            case OP_CTRL: b = bound_join(bound_matrix(op.gate.data(), 2), OpBound{}); break;
+            case OP_SWAP:
+            case OP_PAULI_TENSOR: break;
+            case OP_PAULI_GADGET:
+            case OP_PHASE_GADGET: b.finite = std::isfinite(v); break;
+            case OP_DEPH1: b = bound_channel(CHAN_DEPH1, v); break;
+            case OP_DEPH2: b = bound_channel(CHAN_DEPH2, v); break;
+            case OP_DEPOL1: b = bound_channel(CHAN_DEPOL1, v); break;
+            case OP_DEPOL2: b = bound_channel(CHAN_DEPOL2, v); break;
+            case OP_DAMPING: b = bound_channel(CHAN_DAMPING, v); break;
+        }
+        if (c->isDM && (op.kind == OP_ONE_TARG || op.kind == OP_MANY_TARG || op.kind == OP_CTRL)) {
+            b.grow *= 2;  // U on the ket qubits and conj(U) on the bra qubits
+            b.shrink *= 2;
+        }
+        t = bound_chain(t, b);
+    }
+    return t;
+}
+
+// a state that stands for s during a run: the same amplitudes, in s's precision or, when
+// the run must leave the double-float window, in native FP64 arithmetic on the same
+// storage; its magnitude bounds cover every intermediate state of the run
+static void run_view(State* s, const OpBound& t, bool native, dfs_state_s* view) {
+    static_cast<State&>(*view) = *s;
+    view->copyPending = false;
+    view->rangePending = false;
+    view->rangeDev = nullptr;
+    view->rangeHost = nullptr;
+    view->rangeReady = nullptr;
+    if (native) view->precision = DFS_C128_NATIVE;
+    else range_widen(view, t);
+}
+
 static int check_circuit(const Circuit* c) {
     return c ? DFS_SUCCESS : fail(DFS_ERR_INVALID_ARG, "null circuit");
 }
@@ -945,7 +990,14 @@ int dfs_circuit_apply(dfs_circuit c, dfs_state s, const double* params) {
     if (!rc) rc = check_state_for(c, s);
     if (!rc) rc = check_params(c, params);
     if (rc) return rc;
-    return forward(c, s, params, false);
+    const OpBound t = circuit_bound(c, params);
+    bool native = false;
+    if ((rc = range_decide(s, t, 0.0, &native))) return rc;
+    dfs_state_s view;
+    run_view(s, t, native, &view);
+    rc = forward(c, &view, params, false);
+    range_after(s, t, rc);
+    return rc;
 }
 
 int dfs_circuit_expec(dfs_circuit c, dfs_state initial, const double* params, const double* coeffs,
@@ -960,8 +1012,19 @@ int dfs_circuit_expec(dfs_circuit c, dfs_state initial, const double* params, co
         if (allPaulis[i] > 3) rc = fail(DFS_ERR_INVALID_ARG, "Pauli code %u (expected 0-3)", allPaulis[i]);
     if (rc) return rc;
     c->haveForward = false;
-    if ((rc = ensure_storage(c, initial->precision))) return rc;
+    // the run, its adjoint H psi and the loss stay inside the double-float window, or the
+    // whole run takes native FP64 arithmetic (storage of the same layout)
+    const OpBound t = circuit_bound(c, params);
+    long double sumC = 0;
+    for (unsigned i = 0; i < numTerms; i++) sumC += std::fabs(coeffs[i]);
+    const double lgC = sumC > 0 ? (double)std::log2(sumC) : 0.0;
+    bool native = false;
+    if ((rc = range_decide(initial, t, lgC, &native))) return rc;
+    if (!native && initial->precision == DFS_C128 && 2.0 * (initial->lgHi + t.grow) + lgC + 1.0 > 120.0)
+        native = true;
+    if ((rc = ensure_storage(c, native ? DFS_C128_NATIVE : initial->precision))) return rc;
     if ((rc = dfs_state_copy(static_cast<dfs_state>(c->work), initial))) return rc;
+    range_widen(c->work, t);
     if ((rc = forward(c, c->work, params, true))) return rc;
     c->terms = make_terms(c->numQubits, coeffs, numTerms, allPaulis);
     if (c->isDM) {

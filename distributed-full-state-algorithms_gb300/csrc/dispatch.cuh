@@ -9,12 +9,16 @@
 namespace dfs {
 
 // calls F::template run<P, IT>(args...) for the state's precision and size:
-// 32-bit index maths while the amplitude count fits in 31 bits
+// 32-bit index maths while the amplitude count fits in 31 bits.  A complex128 state
+// whose values the range guard (range.cu) has put outside the double-float window
+// runs the native FP64 instantiation on the same storage.
 template <class F, class... Args>
 int dispatch(const State* s, Args&&... args) {
     bool wide = s->numAmps > (1ull << 31);
     switch (s->precision) {
         case DFS_C128:
+            if (s->forceNative)
+                return wide ? F::template run<PolF64, uint64_t>(args...) : F::template run<PolF64, uint32_t>(args...);
             return wide ? F::template run<PolDF, uint64_t>(args...) : F::template run<PolDF, uint32_t>(args...);
         case DFS_C128_NATIVE:
             return wide ? F::template run<PolF64, uint64_t>(args...) : F::template run<PolF64, uint32_t>(args...);

@@ -47,6 +47,22 @@ struct State {
     // on the compute stream waits for it once (state_acquire)
     cudaEvent_t copyDone = nullptr;
     bool copyPending = false;
+
+    // Magnitude bookkeeping for the double-float policy (complex128 states, range.cu):
+    // log2 bounds on the 2-norm of the amplitude vector, -inf for an all-zero state.
+    // An operation runs with the native FP64 instantiation of its kernel (forceNative,
+    // read by dispatch) when these bounds do not keep its values inside the range
+    // double-float represents, or when a non-finite amplitude may be present.
+    double lgHi = -__builtin_inf(), lgLo = -__builtin_inf();
+    bool nonFinite = false;
+    bool rangeKnown = true;   // false: the bounds are re-measured before the next operation
+    bool rangeFresh = true;   // the bounds come from a measurement, not from propagation
+    bool forceNative = false;
+    // measurement enqueued on the copy stream after an asynchronous upload
+    void* rangeDev = nullptr;
+    void* rangeHost = nullptr;
+    cudaEvent_t rangeReady = nullptr;
+    bool rangePending = false;
 };
 
 // orders the context stream after the state's pending asynchronous transfer
@@ -97,9 +113,55 @@ int dm_deph2(State* s, unsigned q1, unsigned q2, double p);
 int dm_depol1(State* s, unsigned q, double p);
 int dm_depol2(State* s, unsigned q1, unsigned q2, double p, int referenceCompat);
 int dm_damping(State* s, unsigned q, double p);
+// one-sweep density-matrix unitaries (ket and bra halves together)
+int dm_swap(State* s, unsigned q1, unsigned q2);
+int dm_pauli_tensor(State* s, const unsigned* targs, const unsigned* paulis, unsigned k);  // k_sv.cu
+int dm_pauli_gadget(State* s, const unsigned* targs, const unsigned* paulis, unsigned k, double theta);
+int dm_phase_gadget(State* s, const unsigned* targs, unsigned k, double theta);
 int dm_expec_pauli(State* s, const double* coeffs, unsigned numTerms, const unsigned* allPaulis, double* re,
                    double* im);
 int dm_partial_trace(State* in, const unsigned* targs, unsigned k, State* out);
+
+// range.cu -- the double-float policy's magnitude window
+// An operation's effect on the 2-norm: log2 of upper / lower bounds on the factor by
+// which it can grow or shrink the amplitude vector's 2-norm (0, 0 for a unitary), and
+// whether its constants (gate entries, angles, probabilities) are all finite.
+struct OpBound {
+    double grow = 0.0, shrink = 0.0;
+    bool finite = true;
+};
+OpBound bound_matrix(const double* gate, size_t dim);       // Gershgorin bounds on A^dagger A
+OpBound bound_values(const double* absValues, size_t num);  // a normal map with these singular values
+OpBound bound_join(OpBound a, OpBound b);                   // both maps' bounds (direct sum)
+OpBound bound_chain(OpBound a, OpBound b);                  // a then b, for every prefix of the chain
+enum { CHAN_DEPH1, CHAN_DEPH2, CHAN_DEPOL1, CHAN_DEPOL2, CHAN_DEPOL2_COMPAT, CHAN_DAMPING };
+OpBound bound_channel(int kind, double p);                  // a channel's superoperator
+// selects the arithmetic of one operation on s (sets s->forceNative); measures the
+// amplitudes first when the bounds are unknown or too loose to decide
+int range_select(State* s, const OpBound& b);
+// after the operation: propagates the bounds and clears forceNative
+void range_after(State* s, const OpBound& b, int rc);
+// selects the arithmetic of a reduction over s (and t, when given): `lgSum` bounds
+// log2 of the largest partial sum relative to the 2-norm (quadratic: of the norm squared).
+// Without mayMeasure, unknown bounds select the native arithmetic instead of a measurement
+// (which allocates its buffers on first use).
+int range_select_reduce(State* s, State* t, double lgSum, bool quadratic, bool mayMeasure = true);
+// bounds unknown: re-measured before the next operation
+void range_forget(State* s);
+// resolves the bounds and, when a NaN/Inf is only suspected from propagation, measures:
+// afterwards s->nonFinite says whether the content holds one (complex128 states)
+int range_confirm_non_finite(State* s);
+// whether a sequence of maps with the combined bound `b`, and values up to 2^lgExtra
+// times the norm (an adjoint H psi), must run natively on s; leaves s's bounds as they are
+int range_decide(State* s, const OpBound& b, double lgExtra, bool* native);
+// widens s's bounds by a chain's (every prefix of it stays inside)
+void range_widen(State* s, const OpBound& b);
+// exact bounds for a state of known content
+void range_set(State* s, double lgNorm);
+void range_copy(State* dst, const State* src);
+// enqueues a measurement on `stream` after an asynchronous upload (read back lazily)
+int range_measure_async(State* s, cudaStream_t stream);
+void range_release(State* s);
 
 // k_util.cu
 int state_fill_zero(State* s);

@@ -135,6 +135,31 @@ constexpr int kOzShift = 1037;
 // host turns into the per-launch bound DenseParams::fastE: a warp whose groups all meet
 // it encodes with df::encode_words_normal (no tiny/subnormal checks).
 
+// The five accumulators of one output (re, im as an f32x2 pair) as a double-float y + yl
+// in units of accumulator 0: a_0 + a_1 2^-8 + a_2 2^-16 + a_3 2^-24 + a_4 2^-32.  For
+// k <= 5, a_0..a_3 are integers, |a_0| < 2^21 and |a_1 2^-8|, |a_2 2^-16|, |a_3 2^-24|
+// < 2^14.3 (one to four digit products of magnitude at most 192 * 255 each, over K <= 64).
+// Each scaled a_u (u = 1..3) splits exactly, with the rounding constant 1.5 * 2^21, into a
+// multiple of 1/4 and a remainder of at most 1/8: the multiples add exactly to a_0 (the
+// sum S stays below 2^21.1 in steps of 1/4: 24 bits), the remainders (bits 2^-3 .. 2^-24)
+// add exactly to each other, and only the addition of a_4 2^-32 rounds (to at most
+// 2^-26).  S is 0 or at least 1/4 and the remainder r below 1/2, so FastTwoSum
+// renormalises.  18 paired operations, half the rounding error of the two TwoSums (20).
+DEV void ozaki_recombine(const uint64_t (&a)[kOzAccs], uint64_t& y, uint64_t& yl) {
+    const uint64_t C = tc::pk2(0x1.8p21f, 0x1.8p21f);
+    // products by powers of two are exact, so ptxas may fuse them into the additions
+    const uint64_t p1 = tc::mul2(a[1], tc::pk2(0x1p-8f, 0x1p-8f));
+    const uint64_t p2 = tc::mul2(a[2], tc::pk2(0x1p-16f, 0x1p-16f));
+    const uint64_t p3 = tc::mul2(a[3], tc::pk2(0x1p-24f, 0x1p-24f));
+    const uint64_t h1 = tc::sub2(tc::add2(p1, C), C);
+    const uint64_t h2 = tc::sub2(tc::add2(p2, C), C);
+    const uint64_t h3 = tc::sub2(tc::add2(p3, C), C);
+    const uint64_t S = tc::add2(tc::add2(tc::add2(a[0], h1), h2), h3);
+    uint64_t r = tc::add2(tc::add2(tc::sub2(p1, h1), tc::sub2(p2, h2)), tc::sub2(p3, h3));
+    r = tc::fma2(a[4], tc::pk2(0x1p-32f, 0x1p-32f), r);
+    tc::fast_two_sum2(S, r, y, yl);
+}
+
 // the bf16 halves of two floats packed as (lo, hi)
 DEV uint32_t pack_bf16(float lo, float hi) { return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632u); }
 
@@ -279,15 +304,8 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
                         uint64_t a[kOzAccs];
 #pragma unroll
                         for (int u = 0; u < kOzAccs; u++) a[u] = tc::pk2(acc[u][2 * c4], acc[u][2 * c4 + 1]);
-                        uint64_t t, tl, t2, t2l, y, yl;
-                        // products by powers of two are exact, so ptxas may fuse them into the
-                        // additions that follow without changing a bit
-                        tc::two_sum2(a[0], tc::mul2(a[1], tc::pk2(0x1p-8f, 0x1p-8f)), t, tl);
-                        tc::two_sum2(t, tc::mul2(a[2], tc::pk2(0x1p-16f, 0x1p-16f)), t2, t2l);
-                        uint64_t e = tc::add2(tl, t2l);
-                        e = tc::fma2(a[3], tc::pk2(0x1p-24f, 0x1p-24f), e);
-                        e = tc::fma2(a[4], tc::pk2(0x1p-32f, 0x1p-32f), e);
-                        tc::fast_two_sum2(t2, e, y, yl);
+                        uint64_t y, yl;
+                        ozaki_recombine(a, y, yl);
                         df::f2 yr, yi;
                         tc::up2(y, yr.hi, yi.hi);
                         tc::up2(yl, yr.lo, yi.lo);
@@ -470,13 +488,8 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
                             uint64_t a[kOzAccs];
 #pragma unroll
                             for (int u = 0; u < kOzAccs; u++) a[u] = tc::pk2(acc[u][2 * c4], acc[u][2 * c4 + 1]);
-                            uint64_t t, tl, t2, t2l, y, yl;
-                            tc::two_sum2(a[0], tc::mul2(a[1], tc::pk2(0x1p-8f, 0x1p-8f)), t, tl);
-                            tc::two_sum2(t, tc::mul2(a[2], tc::pk2(0x1p-16f, 0x1p-16f)), t2, t2l);
-                            uint64_t e = tc::add2(tl, t2l);
-                            e = tc::fma2(a[3], tc::pk2(0x1p-24f, 0x1p-24f), e);
-                            e = tc::fma2(a[4], tc::pk2(0x1p-32f, 0x1p-32f), e);
-                            tc::fast_two_sum2(t2, e, y, yl);
+                            uint64_t y, yl;
+                            ozaki_recombine(a, y, yl);
                             df::f2 yr, yi;
                             tc::up2(y, yr.hi, yi.hi);
                             tc::up2(yl, yr.lo, yi.lo);
@@ -1185,7 +1198,7 @@ static int dense_tc_run(State* s, const unsigned* targs, const double* g) {
 // 14.3, k = 4 9.0 / 46, k = 5 10.9, k = 6 18.1 / 146; complex64 k = 4 3.17 / 19, k = 5 5.05,
 // k = 6 5.55, while complex64 k = 3 stays on the FP32 CUDA cores (6.0 vs 4.9 TB/s).
 bool dense_tc_supported(const State* s, unsigned k) {
-    if (s->precision == DFS_C128_NATIVE || !ctx().denseTensorCores) return false;
+    if (s->precision == DFS_C128_NATIVE || s->forceNative || !ctx().denseTensorCores) return false;
     if (s->precision == DFS_C64) return k >= 4 && k <= 6;
     return k >= 3 && k <= 6;
 }

@@ -43,28 +43,236 @@ struct RunDeph1 {
 int dm_deph1(State* s, unsigned q, double p) { return dispatch<RunDeph1>(s, s, q, p); }
 
 // local_densitymatrix_twoQubitDephasing, src/local_densitymatrix.hpp:45-60:
-// scale by 1 - 4p/3 where the ket and bra bits of qb1 or of qb2 differ.
+// scale by 1 - 4p/3 where the ket and bra bits of qb1 or of qb2 differ.  Items are the
+// 16 elements of bits (qb1, qb2, qb1+n, qb2+n); the 4 whose ket bits equal their bra bits
+// keep their value and are neither read nor written (1.5 NB moved, not 2 NB).
 template <class P, class IT>
-struct Deph2Op {
-    typename P::R f, one;
-    int q1, q1a, q2, q2a;
-    DEV typename P::V apply(IT j, typename P::V x) const {
-        IT d = ((j >> q1) ^ (j >> q1a)) | ((j >> q2) ^ (j >> q2a));
-        return P::scale((d & 1) ? f : one, x);  // no branch; a product by one is exact
+__global__ void __launch_bounds__(kThreads) k_deph2(typename P::store* __restrict__ a, IT items, QList q, IT m1,
+                                                    IT m2, IT m1a, IT m2a, typename P::R f) {
+    const IT stride = (IT)gridDim.x * kThreads;
+    for (IT k = (IT)blockIdx.x * kThreads + threadIdx.x; k < items; k += stride) {
+        const IT b = insert_zeros(k, q);
+        IT idx[12];
+        typename P::V x[12];
+        int n = 0;
+#pragma unroll
+        for (int e = 0; e < 16; e++) {
+            const int k1 = e & 1, k2 = (e >> 1) & 1, b1 = (e >> 2) & 1, b2 = (e >> 3) & 1;
+            if (k1 == b1 && k2 == b2) continue;
+            idx[n] = b | (k1 ? m1 : 0) | (k2 ? m2 : 0) | (b1 ? m1a : 0) | (b2 ? m2a : 0);
+            x[n] = P::load(a, idx[n]);
+            n++;
+        }
+#pragma unroll
+        for (int e = 0; e < 12; e++) P::save(a, idx[e], P::scale(f, x[e]));
     }
-};
+}
 
 struct RunDeph2 {
     template <class P, class IT>
     static int run(State* s, unsigned q1, unsigned q2, double p) {
         unsigned n = s->numQubits;
-        Deph2Op<P, IT> op{P::mkr(1 - 4 * p / 3), P::mkr(1.0), (int)q1, (int)(q1 + n), (int)q2, (int)(q2 + n)};
-        IT items = (IT)s->numAmps;
-        return launch(k_diag<P, IT, Deph2Op<P, IT>>, items, diag_per<P>(), "twoQubitDephasing", (typename P::store*)s->amps,
-                      items, op);
+        QList q = make_qlist({q1, q2, q1 + n, q2 + n});
+        IT items = (IT)(s->numAmps / 16);
+        return launch(k_deph2<P, IT>, items, 1, "twoQubitDephasing", (typename P::store*)s->amps, items, q,
+                      (IT)(1ull << q1), (IT)(1ull << q2), (IT)(1ull << (q1 + n)), (IT)(1ull << (q2 + n)),
+                      P::mkr(1 - 4 * p / 3));
     }
 };
 int dm_deph2(State* s, unsigned q1, unsigned q2, double p) { return dispatch<RunDeph2>(s, s, q1, q2, p); }
+
+// ------------------------------------------- unitaries on both sides at once
+// distributed_densitymatrix_swapGate / phaseGadget / pauliGadget,
+// src/distributed_densitymatrix.hpp:28-76, apply an operation to the ket qubits and its
+// conjugate to the bra qubits in two sweeps.  The two act on disjoint bits and commute,
+// so each pair is one sweep here.
+
+// swap of (qb1, qb2) and of (qb1+n, qb2+n): within each 16-group of those bits element
+// (k1, k2, b1, b2) goes to (k2, k1, b2, b1); the 12 with k1 != k2 or b1 != b2 move, as 6
+// exchanges (exact, raw storage; 1.5 NB moved)
+template <class S, class IT>
+__global__ void __launch_bounds__(kThreads) k_dm_swap(S* __restrict__ a, IT items, QList q, IT m1, IT m2, IT m1a,
+                                                      IT m2a) {
+    const IT stride = (IT)gridDim.x * kThreads;
+    for (IT k = (IT)blockIdx.x * kThreads + threadIdx.x; k < items; k += stride) {
+        const IT b = insert_zeros(k, q);
+        IT i0[6], i1[6];
+        S x0[6], x1[6];
+        int n = 0;
+#pragma unroll
+        for (int e = 0; e < 16; e++) {
+            const int k1 = e & 1, k2 = (e >> 1) & 1, b1 = (e >> 2) & 1, b2 = (e >> 3) & 1;
+            const int f = k2 | (k1 << 1) | (b2 << 2) | (b1 << 3);
+            if (f <= e) continue;  // fixed points, and each exchange once
+            i0[n] = b | (k1 ? m1 : 0) | (k2 ? m2 : 0) | (b1 ? m1a : 0) | (b2 ? m2a : 0);
+            i1[n] = b | (k2 ? m1 : 0) | (k1 ? m2 : 0) | (b2 ? m1a : 0) | (b1 ? m2a : 0);
+            x0[n] = a[i0[n]];
+            x1[n] = a[i1[n]];
+            n++;
+        }
+#pragma unroll
+        for (int e = 0; e < 6; e++) {
+            a[i0[e]] = x1[e];
+            a[i1[e]] = x0[e];
+        }
+    }
+}
+
+struct RunDmSwap {
+    template <class P, class IT>
+    static int run(State* s, unsigned q1, unsigned q2) {
+        const unsigned n = s->numQubits;
+        if (sizeof(typename P::store) == 8 && q1 >= 1 && q2 >= 1) {
+            // complex64 with qubit 0 untouched: 16-byte elements (two amplitudes), every bit
+            // position one lower (as for the statevector swap)
+            const unsigned b1 = q1 - 1, b2 = q2 - 1, b1a = q1 + n - 1, b2a = q2 + n - 1;
+            QList q = make_qlist({b1, b2, b1a, b2a});
+            IT items = (IT)(s->numAmps / 32);
+            return launch(k_dm_swap<double2, IT>, items, 1, "swapGate", (double2*)s->amps, items, q,
+                          (IT)(1ull << b1), (IT)(1ull << b2), (IT)(1ull << b1a), (IT)(1ull << b2a));
+        }
+        QList q = make_qlist({q1, q2, q1 + n, q2 + n});
+        IT items = (IT)(s->numAmps / 16);
+        using S = typename P::store;
+        return launch(k_dm_swap<S, IT>, items, 1, "swapGate", (S*)s->amps, items, q, (IT)(1ull << q1),
+                      (IT)(1ull << q2), (IT)(1ull << (q1 + n)), (IT)(1ull << (q2 + n)));
+    }
+};
+int dm_swap(State* s, unsigned q1, unsigned q2) { return dispatch<RunDmSwap>(s, s, q1, q2); }
+
+// a diagonal phase chosen by the parities of the ket and the bra bits of a mask:
+// x * k[parity(j & maskKet) | parity(j & maskBra) << 1]
+template <class P, class IT>
+struct DmDiagPhaseOp {
+    typename P::K k[4];
+    IT maskKet, maskBra;
+    DEV typename P::V apply(IT j, typename P::V x) const {
+        // selects, not an indexed load: a runtime index would move k to local memory
+        const int pk = parity(j & maskKet), pb = parity(j & maskBra);
+        const typename P::K kk = pb ? (pk ? k[3] : k[2]) : (pk ? k[1] : k[0]);
+        return P::mul(kk, x);
+    }
+};
+
+struct RunDmDiagPhase {
+    // factor e^{i a} for even and e^{-i a} for odd ket parity, times the same with angle
+    // b for the bra parity
+    template <class P, class IT>
+    static int run(State* s, uint64_t maskKet, double a, double b) {
+        DmDiagPhaseOp<P, IT> op;
+        for (int pk = 0; pk < 2; pk++)
+            for (int pb = 0; pb < 2; pb++) {
+                const double ang = (pk ? -a : a) + (pb ? -b : b);
+                op.k[pk | pb << 1] = P::mk(std::cos(ang), std::sin(ang));
+            }
+        op.maskKet = (IT)maskKet;
+        op.maskBra = (IT)(maskKet << s->numQubits);
+        IT items = (IT)s->numAmps;
+        return launch(k_diag<P, IT, DmDiagPhaseOp<P, IT>>, items, diag_per<P>(), "phaseGadget",
+                      (typename P::store*)s->amps, items, op);
+    }
+};
+
+// ket gadget exp(i theta P) and bra gadget exp(i theta' P) (theta' = theta for an odd
+// number of Ys, else -theta, the reference's choice) on a string with an X or Y, on quads
+// (j, j^Xk, j^Xb, j^Xk^Xb): the ket gadget c + i s P_k, then the bra gadget c + i s' P_b,
+// both in registers, (P x)[j] = i^{#Y} (-1)^{parity((j ^ X) & YZ)} x[j ^ X] on each side.
+// (Factored, 3 complex products per amplitude; the expanded product c^2 + i c s P_k +
+// i c s' P_b - s s' P_k P_b takes 3.5.)
+template <class P, class IT>
+struct DmGadgetOp {
+    typename P::R c;
+    typename P::K kK[2], kB[2];  // i s i^{#Y} (ket), i s' i^{#Y} (bra), and their negations
+    IT xk, xb, yzk, yzb;
+    int topK, topB;  // highest X bit of each side (topK < topB)
+};
+
+template <class P, class IT>
+__global__ void __launch_bounds__(kThreads) k_dm_gadget(typename P::store* __restrict__ a, IT items,
+                                                        DmGadgetOp<P, IT> op) {
+    const IT stride = (IT)gridDim.x * kThreads;
+    for (IT j = (IT)blockIdx.x * kThreads + threadIdx.x; j < items; j += stride) {
+        const IT b = insert_zero(insert_zero(j, op.topK), op.topB);
+        const IT idx[4] = {b, b ^ op.xk, b ^ op.xb, b ^ op.xk ^ op.xb};
+        typename P::V x[4], y[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) x[e] = P::load(a, idx[e]);
+        // the ket gadget, then the bra gadget, in registers: c x + (i s i^{#Y} sign) partner,
+        // the sign that of the partner's index (parity((i ^ X) & YZ) on each side)
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            typename P::A acc = P::first_r(op.c, x[e]);
+            P::mac(acc, parity(idx[e ^ 1] & op.yzk) ? op.kK[1] : op.kK[0], x[e ^ 1]);
+            y[e] = P::get(acc);
+        }
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            typename P::A acc = P::first_r(op.c, y[e]);
+            P::mac(acc, parity(idx[e ^ 2] & op.yzb) ? op.kB[1] : op.kB[0], y[e ^ 2]);
+            P::save(a, idx[e], P::get(acc));
+        }
+    }
+}
+
+struct RunDmGadget {
+    template <class P, class IT>
+    static int run(State* s, uint64_t xk, uint64_t yzk, int numY, double theta) {
+        const unsigned n = s->numQubits;
+        const double th2 = (numY & 1) ? theta : -theta;
+        const double c = std::cos(theta), sn = std::sin(theta), sn2 = std::sin(th2);
+        // i^k times a real r, as (re, im)
+        auto ipow = [](int k, double r, double* re, double* im) {
+            const double tr[4] = {1, 0, -1, 0}, ti[4] = {0, 1, 0, -1};
+            *re = r * tr[k & 3];
+            *im = r * ti[k & 3];
+        };
+        DmGadgetOp<P, IT> op;
+        op.c = P::mkr(c);
+        double re, im;
+        ipow(numY + 1, sn, &re, &im);
+        op.kK[0] = P::mk(re, im);
+        op.kK[1] = P::mk(-re, -im);
+        ipow(numY + 1, sn2, &re, &im);
+        op.kB[0] = P::mk(re, im);
+        op.kB[1] = P::mk(-re, -im);
+        op.xk = (IT)xk;
+        op.xb = (IT)(xk << n);
+        op.yzk = (IT)yzk;
+        op.yzb = (IT)(yzk << n);
+        op.topK = 63 - __builtin_clzll(xk);
+        op.topB = op.topK + (int)n;
+        IT items = (IT)(s->numAmps / 4);
+        return launch(k_dm_gadget<P, IT>, items, 1, "pauliGadget", (typename P::store*)s->amps, items, op);
+    }
+};
+
+// the density-matrix Pauli gadget in one sweep
+int dm_pauli_gadget(State* s, const unsigned* targs, const unsigned* paulis, unsigned k, double theta) {
+    uint64_t xk = 0, yzk = 0;
+    int numY = 0;
+    for (unsigned i = 0; i < k; i++) {
+        if (paulis[i] == 1 || paulis[i] == 2) xk |= 1ull << targs[i];
+        if (paulis[i] == 2 || paulis[i] == 3) yzk ^= 1ull << targs[i];
+        numY += paulis[i] == 2;
+    }
+    if (xk == 0) {
+        // no X or Y on either side: Z..Z phases, exp(i theta Z) on the ket and exp(-i theta Z)
+        // on the bra (no Y, so theta' = -theta); the identity string is a global phase
+        // e^{i theta} e^{-i theta} = 1
+        if (yzk == 0) return DFS_SUCCESS;
+        return dispatch<RunDmDiagPhase>(s, s, yzk, theta, -theta);
+    }
+    return dispatch<RunDmGadget>(s, s, xk, yzk, numY, theta);
+}
+
+// distributed_densitymatrix_phaseGadget, src/distributed_densitymatrix.hpp:66-76: the ket
+// phase gadget with theta and the bra one with -theta, as one diagonal sweep
+int dm_phase_gadget(State* s, const unsigned* targs, unsigned k, double theta) {
+    uint64_t m = 0;
+    for (unsigned i = 0; i < k; i++) m ^= 1ull << targs[i];
+    if (m == 0) return DFS_SUCCESS;  // e^{i theta} e^{-i theta} on every element
+    return dispatch<RunDmDiagPhase>(s, s, m, theta, -theta);
+}
 
 // ---------------------------------------------------------------- quads
 // Items are the four elements (j00, j01, j10, j11) of bits (q+n, q).
@@ -168,30 +376,32 @@ __global__ void __launch_bounds__(kThreads) k_depol2(typename P::store* __restri
                                                      typename P::R c2, typename P::R c3) {
     const IT stride = (IT)gridDim.x * kThreads;
     for (IT k = (IT)blockIdx.x * kThreads + threadIdx.x; k < items; k += stride) {
-        IT b = insert_zeros(k, q);
-        // diagonal elements: (k1,k2) == (b1,b2)
-        IT d[4] = {b, b | m1 | m1a, b | m2 | m2a, b | m1 | m1a | m2 | m2a};
-        typename P::V x[4];
-#pragma unroll
-        for (int i = 0; i < 4; i++) x[i] = P::load(a, d[i]);
-        typename P::A sum = P::from(x[0]);
-        P::add(sum, x[1]);
-        P::add(sum, x[2]);
-        P::add(sum, x[3]);
-        typename P::V tot = P::get(sum);
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            typename P::A acc = P::first_r(w, x[i]);
-            P::mac_r(acc, c2, tot);
-            P::save(a, d[i], P::get(acc));
-        }
-        // off-diagonal elements: the other 12 combinations of the four bits
+        const IT b = insert_zeros(k, q);
+        // all 16 loads issued before the first store (memory-level parallelism)
+        IT idx[16];
+        typename P::V x[16];
 #pragma unroll
         for (int e = 0; e < 16; e++) {
-            int k1 = e & 1, k2 = (e >> 1) & 1, b1 = (e >> 2) & 1, b2 = (e >> 3) & 1;
-            if (k1 == b1 && k2 == b2) continue;
-            IT i = b | (k1 ? m1 : 0) | (k2 ? m2 : 0) | (b1 ? m1a : 0) | (b2 ? m2a : 0);
-            P::save(a, i, P::scale(c3, P::load(a, i)));
+            const int k1 = e & 1, k2 = (e >> 1) & 1, b1 = (e >> 2) & 1, b2 = (e >> 3) & 1;
+            idx[e] = b | (k1 ? m1 : 0) | (k2 ? m2 : 0) | (b1 ? m1a : 0) | (b2 ? m2a : 0);
+            x[e] = P::load(a, idx[e]);
+        }
+        // diagonal elements (k1, k2) == (b1, b2): e = 0, 5, 10, 15
+        typename P::A sum = P::from(x[0]);
+        P::add(sum, x[5]);
+        P::add(sum, x[10]);
+        P::add(sum, x[15]);
+        const typename P::V tot = P::get(sum);
+#pragma unroll
+        for (int e = 0; e < 16; e++) {
+            const int k1 = e & 1, k2 = (e >> 1) & 1, b1 = (e >> 2) & 1, b2 = (e >> 3) & 1;
+            if (k1 == b1 && k2 == b2) {
+                typename P::A acc = P::first_r(w, x[e]);
+                P::mac_r(acc, c2, tot);
+                P::save(a, idx[e], P::get(acc));
+            } else {
+                P::save(a, idx[e], P::scale(c3, x[e]));
+            }
         }
     }
 }
@@ -311,27 +521,81 @@ int dm_expec_pauli(State* s, const double* coeffs, unsigned numTerms, const unsi
 // local_densitymatrix_partialTrace, src/local_densitymatrix.hpp:134-164: output element l
 // sums the 2^k input elements with the traced ket bits equal to the traced bra bits.
 
+template <class P>
+DEV typename P::V sum_value(const typename SumOf<P>::T& s) {
+    typename P::V y;
+    if constexpr (std::is_same<P, PolF32>::value) {
+        y.re = s.re.hi + s.re.lo;
+        y.im = s.im.hi + s.im.lo;
+    } else {
+        y.re = s.re;
+        y.im = s.im;
+    }
+    return y;
+}
+
+// many outputs (4^(n-k) >= 2^20): each thread sums kPtPer outputs at a time, the loads of
+// all of them issued for each traced index before they are added (memory-level parallelism);
+// the traced offsets sel[] sit in shared memory when they fit
+constexpr int kPtPer = 4;
+constexpr int kPtSmemSel = 1024;
+
 template <class P, class IT>
 __global__ void __launch_bounds__(kThreads) k_partial_trace(const typename P::store* __restrict__ in,
                                                             typename P::store* __restrict__ out, IT numOut, QList all,
                                                             const uint64_t* __restrict__ sel, int k) {
     using Sum = typename SumOf<P>::T;
-    const IT stride = (IT)gridDim.x * kThreads;
+    __shared__ uint64_t sSel[kPtSmemSel];
     const IT numTraced = (IT)1 << k;
-    for (IT l = (IT)blockIdx.x * kThreads + threadIdx.x; l < numOut; l += stride) {
-        IT b = insert_zeros(l, all);
+    const bool inSmem = numTraced <= (IT)kPtSmemSel;
+    if (inSmem)
+        for (int t = threadIdx.x; t < (int)numTraced; t += kThreads) sSel[t] = sel[t];
+    __syncthreads();
+    const IT stride = (IT)gridDim.x * (IT)(kThreads * kPtPer);
+    for (IT base = (IT)blockIdx.x * (IT)(kThreads * kPtPer) + threadIdx.x; base < numOut; base += stride) {
+        IT b[kPtPer];
+        Sum s[kPtPer];
+#pragma unroll
+        for (int q = 0; q < kPtPer; q++) {
+            const IT l = base + (IT)(q * kThreads);
+            b[q] = l < numOut ? insert_zeros(l, all) : (IT)0;
+            sum_zero(s[q]);
+        }
+        for (IT t = 0; t < numTraced; t++) {
+            const IT off = (IT)(inSmem ? sSel[t] : __ldg(&sel[t]));
+            typename P::V v[kPtPer];
+#pragma unroll
+            for (int q = 0; q < kPtPer; q++)
+                if (base + (IT)(q * kThreads) < numOut) v[q] = P::load(in, b[q] | off);
+#pragma unroll
+            for (int q = 0; q < kPtPer; q++)
+                if (base + (IT)(q * kThreads) < numOut) sum_add(s[q], v[q], false);
+        }
+#pragma unroll
+        for (int q = 0; q < kPtPer; q++) {
+            const IT l = base + (IT)(q * kThreads);
+            if (l < numOut) P::save(out, l, sum_value<P>(s[q]));
+        }
+    }
+}
+
+// few outputs: a warp per output, its lanes splitting the traced indices, a shuffle
+// reduction at the end
+template <class P, class IT>
+__global__ void __launch_bounds__(kThreads) k_partial_trace_warp(const typename P::store* __restrict__ in,
+                                                                 typename P::store* __restrict__ out, IT numOut,
+                                                                 QList all, const uint64_t* __restrict__ sel, int k) {
+    using Sum = typename SumOf<P>::T;
+    const int lane = threadIdx.x & 31;
+    const IT warps = (IT)gridDim.x * (kThreads / 32);
+    const IT numTraced = (IT)1 << k;
+    for (IT l = (IT)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); l < numOut; l += warps) {
+        const IT b = insert_zeros(l, all);
         Sum s;
         sum_zero(s);
-        for (IT t = 0; t < numTraced; t++) sum_add(s, P::load(in, b | (IT)sel[t]), false);
-        typename P::V y;
-        if constexpr (std::is_same<P, PolF32>::value) {
-            y.re = s.re.hi + s.re.lo;
-            y.im = s.im.hi + s.im.lo;
-        } else {
-            y.re = s.re;
-            y.im = s.im;
-        }
-        P::save(out, l, y);
+        for (IT t = (IT)lane; t < numTraced; t += 32) sum_add(s, P::load(in, b | (IT)__ldg(&sel[t])), false);
+        for (int o = 16; o > 0; o >>= 1) sum_shfl(s, o);
+        if (lane == 0) P::save(out, l, sum_value<P>(s));
     }
 }
 
@@ -356,10 +620,17 @@ struct RunPartialTrace {
         int rc = upload_scratch(sel.data(), sel.size() * sizeof(uint64_t), 0);
         if (rc) return rc;
         IT numOut = (IT)out->numAmps;
-        Launch L = launch_for(numOut, 1, ctx().numSMs);
-        k_partial_trace<P, IT><<<L.grid, L.block, 0, ctx().stream>>>((const typename P::store*)in->amps,
-                                                                       (typename P::store*)out->amps, numOut, q,
-                                                                       (const uint64_t*)ctx().scratch, (int)k);
+        if ((uint64_t)numOut >= (1ull << 20)) {
+            Launch L = launch_for(numOut, kPtPer, ctx().numSMs, 16);
+            k_partial_trace<P, IT><<<L.grid, L.block, 0, ctx().stream>>>((const typename P::store*)in->amps,
+                                                                           (typename P::store*)out->amps, numOut, q,
+                                                                           (const uint64_t*)ctx().scratch, (int)k);
+        } else {
+            Launch L = launch_for((uint64_t)numOut * 32, 1, ctx().numSMs, 16);
+            k_partial_trace_warp<P, IT><<<L.grid, L.block, 0, ctx().stream>>>(
+                (const typename P::store*)in->amps, (typename P::store*)out->amps, numOut, q,
+                (const uint64_t*)ctx().scratch, (int)k);
+        }
         return check_launch("partialTrace");
     }
 };

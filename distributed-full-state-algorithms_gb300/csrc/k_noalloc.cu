@@ -3,12 +3,13 @@
 //
 // Who needs it: callers that must not allocate device (or host) memory at the
 // moment they ask for an expectation value -- code running inside a memory pool
-// or caching allocator that owns every byte of the GPU, latency-critical loops
-// that cannot afford the implicit device synchronisation cudaFree performs, and
-// call sites that are later captured into a CUDA graph.  The ordinary
-// dfs_densitymatrix_expecPauliString grows a device scratch buffer and a pinned
-// staging buffer on demand; this variant uses a fixed, file-scope device array
-// instead and stages nothing on the host.
+// or caching allocator that owns every byte of the GPU, and latency-critical
+// loops that cannot afford the implicit device synchronisation cudaFree
+// performs.  The ordinary dfs_densitymatrix_expecPauliString grows a device
+// scratch buffer and a pinned staging buffer on demand; this variant uses a
+// fixed, file-scope device array instead and stages nothing on the host.  Like
+// the ordinary entry point it is synchronous: it returns after reading the
+// result back into a variable of its own and synchronising the engine's stream.
 //
 // Limits and sharing rules (also stated in include/dfs_gb300.h):
 //  - the array holds kNoAllocSlots = 8192 complex partial sums (128 KiB); a call
@@ -20,8 +21,12 @@
 //    so no slot has to start at zero, but calls whose kernels overlap on the GPU
 //    (different streams or host threads) race on it and must be serialised;
 //  - the first call on each device looks up the array's device address with
-//    cudaGetSymbolAddress; make that first call before any stream capture.
+//    cudaGetSymbolAddress (with the engine's device current); make that first
+//    call before any stream capture;
+//  - a complex128 matrix whose magnitudes the engine has not measured yet is
+//    summed with native FP64 arithmetic (measuring would allocate).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 
 #include "kernels.cuh"
@@ -35,8 +40,9 @@ constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) double2 g_noallocScratch[kNoAllocSlots];
 
-// device address of g_noallocScratch per device ordinal, found once per device
-static void* g_noallocAddr[kNoAllocMaxDevices];
+// device address of g_noallocScratch per device ordinal, found once per device; two
+// threads making a first call at once both store the same address
+static std::atomic<void*> g_noallocAddr[kNoAllocMaxDevices];
 
 struct NoAllocTerms {
     int num;
@@ -73,37 +79,69 @@ __global__ void __launch_bounds__(kThreads) k_expec_dm_noalloc(const typename P:
     }
 }
 
-// one CTA: result = sum of count partials (double-float accumulation, fixed order)
-__global__ void __launch_bounds__(kThreads) k_sum_partials_noalloc(const double2* __restrict__ partials, int count,
-                                                                   double2* __restrict__ result) {
-    SumDF s;
-    sum_zero(s);
-    for (int i = threadIdx.x; i < count; i += kThreads) {
-        double2 v = partials[i];
-        // split each double into two floats exactly enough for a 48-bit sum
-        float rh = (float)v.x, ih = (float)v.y;
-        df::f2 re = {rh, (float)(v.x - (double)rh)}, im = {ih, (float)(v.y - (double)ih)};
-        s.re = dfadd(s.re, re);
-        s.im = dfadd(s.im, im);
-    }
-    s = block_reduce(s);
-    if (threadIdx.x == 0) *result = sum_to_double2(s);
+// double-double: an unevaluated sum hi + lo of two doubles (Knuth TwoSum)
+struct DD {
+    double hi, lo;
+};
+DEV DD dd_add(DD a, DD b) {
+    const double s = a.hi + b.hi;
+    const double bb = s - a.hi;
+    const double e = (a.hi - (s - bb)) + (b.hi - bb);
+    const double lo = e + a.lo + b.lo;
+    const double h = s + lo;
+    return {h, lo - (h - s)};
 }
 
+// one CTA: result = sum of count partials, in double-double and a fixed order (the
+// partials keep the full double range, as the ordinary entry point's host sum does)
+__global__ void __launch_bounds__(kThreads) k_sum_partials_noalloc(const double2* __restrict__ partials, int count,
+                                                                   double2* __restrict__ result) {
+    DD re = {0.0, 0.0}, im = {0.0, 0.0};
+    for (int i = threadIdx.x; i < count; i += kThreads) {
+        const double2 v = partials[i];
+        re = dd_add(re, {v.x, 0.0});
+        im = dd_add(im, {v.y, 0.0});
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        re = dd_add(re, {__shfl_down_sync(0xffffffffu, re.hi, off), __shfl_down_sync(0xffffffffu, re.lo, off)});
+        im = dd_add(im, {__shfl_down_sync(0xffffffffu, im.hi, off), __shfl_down_sync(0xffffffffu, im.lo, off)});
+    }
+    __shared__ DD wr[kThreads / 32], wi[kThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        wr[warp] = re;
+        wi[warp] = im;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < kThreads / 32; w++) {
+            re = dd_add(re, wr[w]);
+            im = dd_add(im, wi[w]);
+        }
+        *result = make_double2(re.hi + re.lo, im.hi + im.lo);
+    }
+}
+
+// the array's device address on the engine's device (which need not be the calling
+// thread's current device)
 static int noalloc_scratch(double2** out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    const int dev = ctx().device;
     if (dev < 0 || dev >= kNoAllocMaxDevices)
         return fail(DFS_ERR_INVALID_ARG, "device ordinal %d is beyond the %d the no-alloc path tracks", dev,
                     kNoAllocMaxDevices);
-    if (!g_noallocAddr[dev]) {
-        void* p = nullptr;
+    void* p = g_noallocAddr[dev].load(std::memory_order_acquire);
+    if (!p) {
+        int cur = 0;
+        cudaError_t e = cudaGetDevice(&cur);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+        if (cur != dev && (e = cudaSetDevice(dev)) != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
         e = cudaGetSymbolAddress(&p, g_noallocScratch);
+        cudaError_t e2 = cur != dev ? cudaSetDevice(cur) : cudaSuccess;
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-alloc scratch)");
-        g_noallocAddr[dev] = p;
+        if (e2 != cudaSuccess) return cuda_fail(e2, "cudaSetDevice");
+        g_noallocAddr[dev].store(p, std::memory_order_release);
     }
-    *out = (double2*)g_noallocAddr[dev];
+    *out = (double2*)p;
     return DFS_SUCCESS;
 }
 
@@ -166,6 +204,7 @@ using namespace dfs;
 
 extern "C" int dfs_densitymatrix_expecPauliString_noalloc(dfs_state s, const double* coeffs, unsigned numTerms,
                                                           const unsigned* allPaulis, double* re, double* im) {
+    DFS_TRACE_CALL();
     if (!s) return fail(DFS_ERR_INVALID_ARG, "null state handle");
     if (!s->isDM) return fail(DFS_ERR_STATE_KIND, "a density matrix is required");
     if (!ctx().initialised) return fail(DFS_ERR_NOT_INITIALISED, "dfs_comm_init() has not been called");
@@ -180,5 +219,16 @@ extern "C" int dfs_densitymatrix_expecPauliString_noalloc(dfs_state s, const dou
     }
     int rc = state_acquire(s);
     if (rc) return rc;
-    return dispatch<RunExpecDMNoAlloc>(s, s, coeffs, numTerms, allPaulis, re, im);
+    // the complex128 magnitude window, as for the ordinary entry point, without measuring
+    if ((rc = range_select_reduce(s, nullptr, 0.5 * s->numQubits, false, false))) return rc;
+    // a NaN or Inf in rho makes the reference's sum NaN (every element is multiplied by
+    // the tensor's, zeros included), as for the ordinary entry point
+    if (s->precision == DFS_C128 && s->rangeKnown && s->nonFinite) {
+        s->forceNative = false;
+        *re = *im = NAN;
+        return DFS_SUCCESS;
+    }
+    rc = dispatch<RunExpecDMNoAlloc>(s, s, coeffs, numTerms, allPaulis, re, im);
+    s->forceNative = false;
+    return rc;
 }

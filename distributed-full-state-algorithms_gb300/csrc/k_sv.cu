@@ -115,7 +115,17 @@ struct SwapOp {
 struct RunSwap {
     template <class P, class IT>
     static int run(State* s, unsigned q1, unsigned q2) {
-        SwapOp<IT> op{(int)std::min(q1, q2), (int)std::max(q1, q2)};
+        const int lo = (int)std::min(q1, q2), hi = (int)std::max(q1, q2);
+        if (sizeof(typename P::store) == 8 && lo >= 1) {
+            // complex64 with qubit 0 untouched: the amplitudes move in adjacent pairs, so the
+            // sweep moves 16-byte elements (two amplitudes) on qubits lo - 1, hi - 1 -- the
+            // complex128 access pattern, twice the bytes per load of 8-byte elements
+            SwapOp<IT> op{lo - 1, hi - 1};
+            IT items = (IT)(s->numAmps / 8);
+            return launch(k_pair_raw<double2, IT, SwapOp<IT>>, items, kRawPairPer, "swapGate", (double2*)s->amps,
+                          items, op);
+        }
+        SwapOp<IT> op{lo, hi};
         IT items = (IT)(s->numAmps / 4);
         using S = typename P::store;
         return launch(k_pair_raw<S, IT, SwapOp<IT>>, items, kRawPairPer, "swapGate", (S*)s->amps, items, op);
@@ -200,8 +210,10 @@ struct DiagSignOp {
 };
 
 struct RunPauli {
+    // extraPow: a further factor i^extraPow on the tensor (its density-matrix form)
     template <class P, class IT>
-    static int run(State* s, const unsigned* targs, const unsigned* paulis, unsigned k, int gadget, double theta) {
+    static int run(State* s, const unsigned* targs, const unsigned* paulis, unsigned k, int gadget, double theta,
+                   int extraPow) {
         uint64_t mX = 0, mYZ = 0;
         int numY = 0, top = -1;
         for (unsigned i = 0; i < k; i++) {
@@ -229,19 +241,25 @@ struct RunPauli {
                           items, op);
         }
         IT items = (IT)(s->numAmps / 2);
-        if (!gadget) {
-            PauliTensorOp<IT> op{(IT)mX, (IT)mYZ, top, numY & 3};
+        // The reference forms the tensor as 0 * psi[j] + P psi[j] (thisAmpFac = 0,
+        // src/distributed_statevector.hpp:279-284), so a NaN or Inf amplitude leaves NaN at
+        // its own index too; for a state that may hold one, the tensor takes that arithmetic
+        // form (the gadget kernel with cos = 0, sin = 1 and no extra factor i) instead of the
+        // exact permutation.
+        const bool ieee = s->forceNative && s->nonFinite;
+        if (!gadget && !ieee) {
+            PauliTensorOp<IT> op{(IT)mX, (IT)mYZ, top, (numY + extraPow) & 3};
             return launch(k_pair_raw<S, IT, PauliTensorOp<IT>>, items, kRawPairPer, "pauliTensor", (S*)s->amps, items, op);
         }
         PauliGadgetOp<P, IT> op;
-        op.c = P::mkr(std::cos(theta));
-        op.sn = P::mkr(std::sin(theta));
+        op.c = P::mkr(gadget ? std::cos(theta) : 0.0);
+        op.sn = P::mkr(gadget ? std::sin(theta) : 1.0);
         op.maskX = (IT)mX;
         op.maskYZ = (IT)mYZ;
         op.top = top;
-        op.powY = (numY + 1) & 3;
+        op.powY = gadget ? (numY + 1) & 3 : (numY + extraPow) & 3;
         op.pX = __builtin_parityll(mX & mYZ);
-        const double sn = std::sin(theta);
+        const double sn = gadget ? std::sin(theta) : 1.0;
         const double kre[4] = {sn, 0.0, -sn, 0.0}, kim[4] = {0.0, sn, 0.0, -sn};  // sn i^k
         op.kp = P::mk(kre[op.powY], kim[op.powY]);
         op.kn = P::mk(-kre[op.powY], -kim[op.powY]);
@@ -250,7 +268,31 @@ struct RunPauli {
     }
 };
 int sv_pauli(State* s, const unsigned* targs, const unsigned* paulis, unsigned k, int gadget, double theta) {
-    return dispatch<RunPauli>(s, s, targs, paulis, k, gadget, theta);
+    return dispatch<RunPauli>(s, s, targs, paulis, k, gadget, theta, 0);
+}
+
+// distributed_densitymatrix_pauliTensor, src/distributed_densitymatrix.hpp:36-50: P on the
+// ket qubits, P on the bra qubits, then a negation for an odd number of Ys.  The three
+// factors i^{#Y} i^{#Y} (-1)^{#Y} make one, so this is the tensor of the doubled string
+// (targets ++ targets + n) with its own i^{2 #Y} cancelled: one exact sweep.
+int dm_pauli_tensor(State* s, const unsigned* targs, const unsigned* paulis, unsigned k) {
+    std::vector<unsigned> t(targs, targs + k), p(paulis, paulis + k);
+    int numY = 0;
+    for (unsigned i = 0; i < k; i++) numY += paulis[i] == 2;
+    if (s->forceNative && s->nonFinite) {
+        // NaN/Inf present: the reference's three steps, each tensor in its arithmetic form
+        // (a NaN spreads over the ket and the bra partners as it does there)
+        int rc = sv_pauli(s, targs, paulis, k, 0, 0.0);
+        for (unsigned& q : t) q += s->numQubits;
+        if (!rc) rc = sv_pauli(s, t.data(), paulis, k, 0, 0.0);
+        if (!rc && (numY & 1)) rc = state_scale_real(s, -1.0);
+        return rc;
+    }
+    for (unsigned i = 0; i < k; i++) {
+        t.push_back(targs[i] + s->numQubits);
+        p.push_back(paulis[i]);
+    }
+    return dispatch<RunPauli>(s, s, t.data(), p.data(), 2 * k, 0, 0.0, (2 * numY) & 3);
 }
 
 // ------------------------------------------------------------ phase gadget

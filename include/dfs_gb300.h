@@ -135,6 +135,22 @@ int dfs_state_set_classical(dfs_state s, uint64_t index);
  * unit 2-norm.  Replaces setRandomAmps, tests/test_utilities.hpp:438-448. */
 int dfs_state_set_random(dfs_state s, uint64_t seed, int normalise);
 
+/* Magnitude window of the DFS_C128 arithmetic (no reference counterpart).  The
+ * reference keeps every amplitude as an IEEE double (src/types.hpp:26-38); DFS_C128
+ * keeps that storage but computes in pairs of floats, which represent values only
+ * within the float exponent range: results below 2^-75 in magnitude flush to zero,
+ * values of 2^128 and above, NaN and Inf are not representable.  The engine therefore
+ * keeps log2 bounds on each complex128 state's 2-norm -- measured on the device after
+ * any upload (set_amps, set_raw and their asynchronous forms, state files, and after
+ * dfs_state_device_ptr hands the buffer out), propagated through every operation by its
+ * norm growth -- and runs an operation with native FP64 arithmetic on the same storage
+ * whenever its values could leave [2^-30 of the largest component, 2^120] or a
+ * non-finite value may be present.  Results then follow IEEE double semantics like the
+ * reference's, NaN positions included.  This call reports the bounds (log2 of the
+ * 2-norm; -inf for a zero state) and flags: bit 0 a NaN or Inf may be present, bit 1 the
+ * next operation takes the native arithmetic.  DFS_ERR_PRECISION for other precisions. */
+int dfs_state_magnitude(dfs_state s, double* log2_norm_hi, double* log2_norm_lo, int* flags);
+
 /* Self-test of the device-side failure detection (no reference counterpart): one
  * kernel spins, as the batched kernel's team barrier does, on a word nothing writes
  * until `seconds` have passed by the global timer, and waits, as the tensor-core
@@ -218,6 +234,10 @@ int dfs_densitymatrix_expecPauliString(dfs_state s, const double* coeffs, unsign
 /* distributed_densitymatrix_partialTrace, src/distributed_densitymatrix.hpp:347-406: creates the
  * reduced density matrix of n - num_targets qubits (same precision) in *out */
 int dfs_densitymatrix_partialTrace(dfs_state s, const unsigned* targets, unsigned num_targets, dfs_state* out);
+/* the same reduction into an existing density matrix of n - num_targets qubits and the same
+ * precision (no reference counterpart: the reference returns a new DensityMatrix by value;
+ * this form lets a caller reuse the output's memory across calls) */
+int dfs_densitymatrix_partialTrace_into(dfs_state s, const unsigned* targets, unsigned num_targets, dfs_state out);
 
 /* ----------------------------------------------------------- additions */
 
@@ -234,17 +254,21 @@ int dfs_densitymatrix_trace(dfs_state s, double* out_re, double* out_im);
 
 /* dfs_densitymatrix_expecPauliString without any memory allocation.  No counterpart in the
  * reference.  For callers that cannot allocate at the point of the call: code whose device
- * memory is owned by a pool or caching allocator, loops that cannot afford the device
- * synchronisation cudaFree implies, and call sites captured into CUDA graphs.  The ordinary
- * entry point grows a device scratch buffer and pinned host staging on demand; this one keeps
- * its partial sums in a fixed 128 KiB device array (8192 complex slots) compiled into the
- * library, which every GPU that loads the library holds until the process exits.  A call on an
- * n-qubit matrix needs num_terms * chunks + 1 slots, chunks = ceil(2^n / max(4096, 2^n/256))
- * (1 for n <= 12); larger requests return DFS_ERR_TOO_LARGE.  All calls share the array: each
- * call writes every slot it reads, but calls that overlap on the GPU (other streams or threads)
- * race and must be serialised by the caller.  The first call on each device looks the array's
- * address up with cudaGetSymbolAddress, so make it before any stream capture begins.  Results
- * equal dfs_densitymatrix_expecPauliString's within rounding. */
+ * memory is owned by a pool or caching allocator, and loops that cannot afford the device
+ * synchronisation cudaFree implies.  The ordinary entry point grows a device scratch buffer
+ * and pinned host staging on demand; this one keeps its partial sums in a fixed 128 KiB
+ * device array (8192 complex slots) compiled into the library, which every GPU that loads the
+ * library holds until the process exits.  A call on an n-qubit matrix needs
+ * num_terms * chunks + 1 slots, chunks = ceil(2^n / max(4096, 2^n/256)) (1 for n <= 12);
+ * larger requests return DFS_ERR_TOO_LARGE.  All calls share the array: each call writes
+ * every slot it reads, but calls that overlap on the GPU (other streams or threads) race and
+ * must be serialised by the caller.  The call is synchronous, like the ordinary one: it reads
+ * the result back and synchronises the engine's stream before it returns.  The first call on
+ * each device looks the array's address up with cudaGetSymbolAddress (with the engine's
+ * device current), so make it before any stream capture begins.  A complex128 matrix whose
+ * magnitudes the engine has not yet measured (right after an upload) is summed with native
+ * FP64 arithmetic, since measuring would allocate.  Results equal
+ * dfs_densitymatrix_expecPauliString's within rounding. */
 int dfs_densitymatrix_expecPauliString_noalloc(dfs_state s, const double* coeffs, unsigned num_terms,
                                                const unsigned* all_paulis, double* out_re, double* out_im);
 

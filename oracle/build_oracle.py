@@ -13,6 +13,9 @@ Two shared libraries:
 
 Flags follow the reference's ``compile.sh``: ``-O3 -fopenmp`` plus the native
 CPU tuning flag of the host architecture.
+
+The reference checkout is read from ``$DFS_REFERENCE_CHECKOUT`` (default
+``/root/reference``), or from ``--reference PATH`` when run as a script.
 """
 from __future__ import annotations
 
@@ -24,7 +27,7 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REFERENCE_CHECKOUT = Path("/root/reference")
+REFERENCE_CHECKOUT = Path(os.environ.get("DFS_REFERENCE_CHECKOUT", "/root/reference"))
 REF_DIR = HERE / "_ref"
 BUILD_DIR = HERE / "_build"
 
@@ -88,4 +91,6 @@ def build(force: bool = False, verbose: bool = True) -> None:
 
 
 if __name__ == "__main__":
+    if "--reference" in sys.argv:
+        REFERENCE_CHECKOUT = Path(sys.argv[sys.argv.index("--reference") + 1])
     build(force="--force" in sys.argv)

@@ -134,6 +134,23 @@ def test_partial_trace(dfs, oracle, prec, rng):
         assert rel_err(out.getAllVecAmps(), want) <= TOL[prec]
 
 
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_partial_trace_many_outputs(dfs, oracle, prec, rng):
+    """11 qubits with one traced qubit: 4^10 outputs, the kernel that gives each thread
+    several outputs (the few-output kernel gives each output a warp: covered above)."""
+    n = 11
+    for t in ([0], [10], [5]):
+        a = gaussian_state(rng, 1 << (2 * n))
+        rho = dfs.DensityMatrix(n, precision=prec)
+        rho.setAmps(a)
+        a = rho.getAllVecAmps()
+        out = dfs.distributed_densitymatrix_partialTrace(rho, t)
+        assert rel_err(out.getAllVecAmps(), oracle.dm_partial_trace(a, t)) <= TOL[prec]
+        into = dfs.DensityMatrix(n - 1, precision=prec)
+        dfs.distributed_densitymatrix_partialTrace(rho, t, out=into)
+        assert rel_err(into.getAllVecAmps(), oracle.dm_partial_trace(a, t)) <= TOL[prec]
+
+
 def test_trace_and_matrix_view(dfs, rng):
     n = 4
     m = gaussian_matrix(rng, 1 << n)
