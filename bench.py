@@ -22,7 +22,6 @@ from __future__ import annotations
 import argparse
 import json
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -41,7 +40,6 @@ NUM_QUBITS = 30
 NUM_GATES = 200
 CIRCUIT_SEED = 20240611
 STATE_SEED = 77
-REF_SAMPLE_GATES = 6
 # differentiation form: 24-qubit ansatz of 20 layers x 24 Pauli gadgets, H of 100 terms
 ADJ_QUBITS, ADJ_LAYERS, ADJ_PER_LAYER, ADJ_TERMS = 24, 20, 24, 100
 # batched form: 512 circuits of 10..22 qubits, 50 gates each, H of 32 terms
@@ -62,8 +60,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the e2e, FP32 and native-FP64 legs")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the adjoint, batched and 32-qubit precision legs")
-    ap.add_argument("--legs", default="adjoint,batched,precision32,fusion,dm12",
-                    help="comma-separated forms to run (adjoint, batched, precision32, fusion, dm12)")
+    ap.add_argument("--legs", default="adjoint,batched,precision32,fusion,dm12,dm15",
+                    help="comma-separated forms to run (adjoint, batched, precision32, fusion, dm12, dm15)")
     ap.add_argument("--form-scale", default="full", choices=["full", "small"],
                     help="small: the forms at reduced sizes, for profiling captures")
     ap.add_argument("--batch-shape", default=None,
@@ -170,13 +168,15 @@ def any_rank(flag: bool, world: int) -> bool:
     return float(t.item()) > 0
 
 
-def roofline_traffic(kind: str):
-    """dram read+write bytes per launch of `kind` from the committed ncu summary."""
-    f = ROOT / "profiles" / "ncu_sv30_gate_mix.md"
-    if not f.exists():
+def roofline_traffic(kind: str, qubits: int):
+    """DRAM read+write bytes per launch of `kind` (ncu, profiles/traffic.json), scaled from
+    the capture's state size to this one; None without a capture of that kind."""
+    f = ROOT / "profiles" / "traffic.json"
+    try:
+        t = json.loads(f.read_text())
+        return float(t["bytes_per_launch_at_capture"][kind]) * 2.0 ** (qubits - int(t["capture_qubits"]))
+    except (OSError, KeyError, ValueError):
         return None
-    m = re.search(rf"traffic_bytes_per_launch\[{re.escape(kind)}\]\s*=\s*([0-9.eE+]+)", f.read_text())
-    return float(m.group(1)) if m else None
 
 
 def measured_peak():
@@ -191,19 +191,54 @@ def measured_peak():
 
 # ------------------------------------------------------- reference arm
 
-def reference_arm(args, circuits):
-    """The reference's CPU implementation on the host cores, same workload."""
-    from oracle import build_oracle
+def kinds_of(gates):
+    """The circuit's gates by kind, in circuit order."""
+    by_kind = {}
+    for g in gates:
+        by_kind.setdefault(g.kind, []).append(g)
+    return by_kind
+
+
+def reference_sample(run_gate, gates, steps, warmup):
+    """Times the reference on a stratified sample of the circuit: step i runs the i-th
+    gate of every kind the circuit holds (cyclically, in circuit order), so each step
+    covers the whole mix.  The circuit's rate is its gate count over
+    sum_kind count_kind * mean_seconds_kind.  Returns (gates/s, details)."""
+    by_kind = kinds_of(gates)
+    secs = {k: [] for k in by_kind}
+    t_steps = []
+    for s in range(warmup + steps):
+        t_step = 0.0
+        for kind, gs in by_kind.items():
+            g = gs[s % len(gs)]
+            t0 = time.perf_counter()
+            run_gate(g)
+            dt = time.perf_counter() - t0
+            if s >= warmup:
+                secs[kind].append(dt)
+                t_step += dt
+        if s >= warmup:
+            t_steps.append(t_step)
+    counts = {k: len(v) for k, v in by_kind.items()}
+    mean = {k: statistics.fmean(v) for k, v in secs.items()}
+    full = sum(counts[k] * mean[k] for k in counts)
+    details = {
+        "sample": f"stratified: each step runs one gate of each of the {len(counts)} kinds of the "
+                  f"{len(gates)}-gate circuit (the i-th of its kind at step i)",
+        "kind_counts": counts,
+        "kind_seconds": mean,
+        "sampled_gates": sum(len(v) for v in secs.values()),
+        "sampled_seconds": sum(t_steps),
+        "seconds_per_sampled_step": statistics.fmean(t_steps),
+        "full_circuit_s_extrapolated": full,
+    }
+    return len(gates) / full, details
+
+
+def reference_backend(circuits, n):
+    """The reference build (oracle/_ref) with the seeded state, else the C restatement."""
     from oracle.oracle import Oracle, Reference
-    cores = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    os.environ.setdefault("OMP_PROC_BIND", "true")
-    os.environ.setdefault("OMP_WAIT_POLICY", "active")
-    n = args.qubits
-    gates = circuits.gate_mix(n, args.gates, CIRCUIT_SEED)
-    sample = gates[:REF_SAMPLE_GATES]
     amps = seeded_host_state(n, STATE_SEED)
-    kind = "reference"
     try:
         backend = Reference()
         h = backend.new_state(amps, False)
@@ -211,32 +246,40 @@ def reference_arm(args, circuits):
 
         def run_gate(g):
             run_reference_gate(backend, h, g)
-    except Exception:
-        kind = "port"
-        backend = Oracle()
-        h = None
 
-        def run_gate(g):
-            circuits.apply_to(backend, amps, [g])
-    for _ in range(args.warmup):
-        for g in sample:
-            run_gate(g)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        for g in sample:
-            run_gate(g)
-    dt = time.perf_counter() - t0
-    if h is not None:
-        backend.free_state(h, False)
-    value = len(sample) * args.steps / dt
+        return "reference", run_gate, lambda: backend.free_state(h, False)
+    except Exception:
+        orc = Oracle()
+
+        def run_port(g):
+            circuits.apply_to(orc, amps, [g])
+
+        return "port", run_port, lambda: None
+
+
+def reference_arm(args, circuits):
+    """The reference's CPU implementation on the host cores, same workload: the same
+    30-qubit seeded state and 200-gate circuit, timed on a stratified sample of it."""
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    os.environ.setdefault("OMP_PROC_BIND", "true")
+    os.environ.setdefault("OMP_WAIT_POLICY", "active")
+    n = args.qubits
+    gates = circuits.gate_mix(n, args.gates, CIRCUIT_SEED)
+    kind, run_gate, free = reference_backend(circuits, n)
+    value, det = reference_sample(run_gate, gates, args.steps, args.warmup)
+    free()
+    threads = int(os.environ["OMP_NUM_THREADS"])
     return {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "gates/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": det["seconds_per_sampled_step"] * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "qubits": n, "gates_per_step": len(sample),
-                   "sample": f"first {len(sample)} gates of the {args.gates}-gate circuit per step"},
-        "cpu_baseline": {"value": value, "unit": "gates/s", "cores": int(os.environ["OMP_NUM_THREADS"]),
-                         "kind": kind, "sample": f"first {len(sample)} gates of the circuit, {n} qubits"},
+        "config": {"workload": WORKLOAD, "qubits": n, "gates_per_step": len(det["kind_counts"]),
+                   "circuit_gates": len(gates), "circuit_seed": CIRCUIT_SEED, "precision": "c128",
+                   "state": "seeded N(0,1), normalised", "sample": det["sample"]},
+        "reference_timing": det,
+        "cpu_baseline": {"value": value, "unit": "gates/s", "cores": threads, "kind": kind,
+                         "sample": det["sample"] + f", {args.steps} timed steps, {n} qubits"},
         "e2e": {"value": value, "unit": "gates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -377,7 +420,7 @@ def gpu_arm(args, world, rank, local):
         "hbm_gbs_algorithmic": algo_gbs,
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": roofline_traffic(dominant), "algorithmic_bytes_per_launch": dom_bytes},
+                     "traffic": roofline_traffic(dominant, n), "algorithmic_bytes_per_launch": dom_bytes},
         "kernels": kernels,
         "gpu_launches": sum(d["launches"] for d in per_kind.values()),
         "clocks": clock_info,
@@ -473,7 +516,7 @@ def gpu_arm(args, world, rank, local):
         result["cpu_baseline"] = cpu_baseline(args, circuits, gates)
     if not args.no_forms:
         legs = {"adjoint": adjoint_leg, "batched": batch_leg, "precision32": precision_leg, "fusion": fusion_leg,
-                "dm12": dm_leg}
+                "dm12": dm_leg, "dm15": dm_kernels_leg}
         for name in [x for x in args.legs.split(",") if x]:
             if name not in legs:
                 result[name] = {"error": "unknown leg"}
@@ -671,6 +714,72 @@ def run_reference_dm_op(ref, h, g):
         raise ValueError(g.kind)
 
 
+def dm_kernels_leg(dfs, circuits, small=False):
+    """Every density-matrix kernel on a 15-qubit complex128 matrix (a 30-qubit vector,
+    16 GiB, far above L2), each timed with CUDA events on the engine stream: ms per call,
+    algorithmic bytes (read + write of the elements the operation can change) per second
+    and the fraction of the measured copy bandwidth."""
+    import torch
+    n = 12 if small else 15
+    N, B = 1 << (2 * n), 16
+    rng = np.random.default_rng(15)
+    peak, peak_kind = measured_peak()
+    rho = dfs.DensityMatrix(n)
+    rho.setRandomAmps(seed=5, normalise=True)
+    u1, u2, u3 = (circuits.haar_unitary(rng, d) for d in (2, 4, 8))
+    red1, red3 = dfs.DensityMatrix(n - 1), dfs.DensityMatrix(n - 3)  # partialTrace outputs, reused
+    coeffs, paulis = circuits.pauli_sum(n, 16, seed=3)
+    p = 0.05
+    cases = [
+        ("oneQubitDephasing", "Deph1Op (k_pair)", N * B, lambda: dfs.distributed_densitymatrix_oneQubitDephasing(rho, 3, p)),
+        ("twoQubitDephasing", "k_deph2", 1.5 * N * B, lambda: dfs.distributed_densitymatrix_twoQubitDephasing(rho, 5, 9, p)),
+        ("twoQubitDephasing (qubit 0)", "k_deph2", 1.5 * N * B,
+         lambda: dfs.distributed_densitymatrix_twoQubitDephasing(rho, 0, 9, p)),
+        ("oneQubitDepolarising", "k_quad<Depol1Op>", 2 * N * B, lambda: dfs.distributed_densitymatrix_oneQubitDepolarising(rho, 5, p)),
+        ("twoQubitDepolarising", "k_depol2", 2 * N * B, lambda: dfs.distributed_densitymatrix_twoQubitDepolarising(rho, 1, 11, p)),
+        ("damping", "k_quad<DampingOp>", 2 * N * B, lambda: dfs.distributed_densitymatrix_damping(rho, 7, p)),
+        ("manyTargGate k=1", "superoperator on 2 targets (k_many_targ_reg)", 2 * N * B,
+         lambda: dfs.distributed_densitymatrix_manyTargGate(rho, [4], u1)),
+        ("manyTargGate k=2", "superoperator on 4 targets (tensor cores)", 2 * N * B,
+         lambda: dfs.distributed_densitymatrix_manyTargGate(rho, [2, 10], u2)),
+        ("manyTargGate k=3", "U then conj(U) (two 3-target sweeps)", 4 * N * B,
+         lambda: dfs.distributed_densitymatrix_manyTargGate(rho, [0, 6, 12], u3)),
+        ("swapGate", "k_dm_swap", 1.5 * N * B, lambda: dfs.distributed_densitymatrix_swapGate(rho, 6, 13)),
+        ("swapGate (qubit 0)", "k_dm_swap", 1.5 * N * B, lambda: dfs.distributed_densitymatrix_swapGate(rho, 0, 13)),
+        ("pauliTensor", "doubled string (k_pair_raw<PauliTensorOp>)", 2 * N * B,
+         lambda: dfs.distributed_densitymatrix_pauliTensor(rho, [1, 6, 8], [1, 2, 3])),
+        ("pauliGadget", "k_dm_gadget", 2 * N * B, lambda: dfs.distributed_densitymatrix_pauliGadget(rho, [1, 6, 8], [1, 2, 3], 0.3)),
+        ("phaseGadget", "k_diag<DmDiagPhaseOp>", 2 * N * B, lambda: dfs.distributed_densitymatrix_phaseGadget(rho, [3, 9], 0.4)),
+        ("expecPauliString (16 terms)", "k_expec_dm", 16 * (1 << n) * B,
+         lambda: dfs.distributed_densitymatrix_expecPauliString(rho, coeffs, paulis)),
+        ("partialTrace (1 qubit)", "k_partial_trace", (N // 2 + N // 4) * B,
+         lambda: dfs.distributed_densitymatrix_partialTrace(rho, [4], out=red1)),
+        ("partialTrace (3 qubits)", "k_partial_trace", (N // 8 + N // 64) * B,
+         lambda: dfs.distributed_densitymatrix_partialTrace(rho, [0, 7, 13], out=red3)),
+    ]
+    stream = torch.cuda.current_stream()
+    out = {"workload": f"{n}-qubit density matrix, c128 ({N} amplitudes, {N * B / 2**30:.0f} GiB)",
+           "peak_gbs": peak, "peak_kind": peak_kind, "kernels": {}}
+    for name, kernel, nbytes, fn in cases:
+        fn()  # warm-up (and the first call's host set-up)
+        times = []
+        for _ in range(3):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            times.append(a.elapsed_time(b))
+        ms = statistics.median(times)
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        out["kernels"][name] = {"kernel": kernel, "ms": ms, "algorithmic_bytes": nbytes, "gbs": gbs,
+                                "frac": gbs / peak}
+    rho.free()
+    red1.free()
+    red3.free()
+    return out
+
+
 def dm_leg(dfs, circuits, small=False):
     """The plain FP64 density-matrix workflow at 12 qubits: rho = G G^dagger / tr, 10 layers
     of a 2-target Haar unitary and the five channels, expecPauliString over 64 strings and
@@ -736,37 +845,20 @@ def dm_leg(dfs, circuits, small=False):
 
 
 def cpu_baseline(args, circuits, gates):
-    """The reference's CPU code (oracle/_ref) on the host cores: the first
-    REF_SAMPLE_GATES gates of the same circuit on the same-size state."""
+    """The reference's CPU code (oracle/_ref) on the host cores: the same circuit on the
+    same-size state, timed on the stratified sample of reference_sample (two steps after
+    one warm-up step: every kind of the mix, about 10-30 s of CPU work)."""
     try:
-        from oracle.oracle import Oracle, Reference
+        kind, run_gate, free = reference_backend(circuits, args.qubits)
     except Exception as e:  # pragma: no cover
         return {"value": None, "error": str(e)}
+    value, det = reference_sample(run_gate, gates, 2, 1)
+    free()
     cores = os.cpu_count() or 1
-    n = args.qubits
-    sample = gates[:REF_SAMPLE_GATES]
-    amps = seeded_host_state(n, STATE_SEED)
-    try:
-        ref = Reference()
-        kind = "reference"
-    except Exception:
-        ref = None
-        kind = "port"
-    if ref is not None:
-        h = ref.new_state(amps, False)
-        del amps
-        t0 = time.perf_counter()
-        for g in sample:
-            run_reference_gate(ref, h, g)
-        dt = time.perf_counter() - t0
-        ref.free_state(h, False)
-    else:
-        orc = Oracle()
-        t0 = time.perf_counter()
-        circuits.apply_to(orc, amps, sample)
-        dt = time.perf_counter() - t0
-    return {"value": len(sample) / dt, "unit": "gates/s", "cores": int(os.environ.get("OMP_NUM_THREADS", cores)),
-            "kind": kind, "sample": f"first {len(sample)} gates of the circuit on the {n}-qubit state"}
+    return {"value": value, "unit": "gates/s", "cores": int(os.environ.get("OMP_NUM_THREADS", cores)),
+            "kind": kind, "sample": det["sample"] + f", 2 timed steps, {args.qubits} qubits",
+            "kind_counts": det["kind_counts"], "kind_seconds": det["kind_seconds"],
+            "full_circuit_s_extrapolated": det["full_circuit_s_extrapolated"]}
 
 
 def main():
