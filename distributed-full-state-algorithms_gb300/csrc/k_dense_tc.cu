@@ -356,7 +356,9 @@ struct WsShape;
 template <>
 struct WsShape<3> {
     static constexpr int SPR = 2, EPQ = 1, kMinBlocks = 2;
-    static constexpr uint32_t kAccCols = 128;  // 5 x 16 used
+    static constexpr int NB = 3;                 // pipeline depth: A buffers and accumulator sets
+    static constexpr uint32_t kAccCols = 80;     // one accumulator set: 5 x 16 columns
+    static constexpr uint32_t kTmemCols = 256;   // NB sets, rounded up to a power of two
 };
 template <int KT>
 constexpr int ws_threads() {
@@ -371,17 +373,17 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
     constexpr int D = S::D, R = S::R;
     constexpr int kSlicers = 128 * W::SPR, kEpi = 128 * W::EPQ, kThreadsAll = ws_threads<KT>();
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* sB = smem + 2 * kOzSlices * S::A16;
-    __shared__ __align__(8) uint64_t fullA[2], issued[2], mmaDone[2], accFree[2], drain;
+    unsigned char* sB = smem + W::NB * kOzSlices * S::A16;
+    __shared__ __align__(8) uint64_t fullA[W::NB], issued[W::NB], mmaDone[W::NB], accFree[W::NB], drain;
     __shared__ uint32_t tmemSlot;
-    __shared__ uint32_t sE[2][128];
+    __shared__ uint32_t sE[W::NB][128];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     for (int i = tid; i < (int)(kOzBCopies * kOzSlices * S::B16 / 16); i += kThreadsAll)
         reinterpret_cast<uint4*>(sB)[i] = bsl[i];
-    if (warp == 0) tc::tmem_alloc<2 * W::kAccCols>(&tmemSlot);
+    if (warp == 0) tc::tmem_alloc<W::kTmemCols>(&tmemSlot);
     if (tid == 0) {
-        for (int b = 0; b < 2; b++) {
+        for (int b = 0; b < W::NB; b++) {
             tc::mbar_init(&fullA[b], kSlicers);
             tc::mbar_init(&issued[b], 1);
             tc::mbar_init(&mmaDone[b], 1);
@@ -411,9 +413,9 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
         uint4 cur[H], nxt[H];
         load(0, cur);
         for (int i = 0; i < myTiles; i++) {
-            const int b = i & 1;
-            const uint32_t k = (uint32_t)i >> 1;
-            if (i >= 2 && !(ok = tc::mbar_wait(&accFree[b], (k - 1) & 1, kTcWaitLimit))) break;
+            const int b = i % W::NB;
+            const uint32_t k = (uint32_t)(i / W::NB);
+            if (i >= W::NB && !(ok = tc::mbar_wait(&accFree[b], (k - 1) & 1, kTcWaitLimit))) break;
             uint32_t E32 = 0;
 #pragma unroll
             for (int c = 0; c < H; c++) E32 = max(E32, max(exp_field(cur[c].y), exp_field(cur[c].w)));
@@ -455,8 +457,8 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
         const int ew = warp - kSlicers / 32, cg = ew >> 2;
         const int row = (ew & 3) * 32 + lane;
         for (int i = 0; i < myTiles; i++) {
-            const int b = i & 1;
-            const uint32_t k = (uint32_t)i >> 1;
+            const int b = i % W::NB;
+            const uint32_t k = (uint32_t)(i / W::NB);
             if (!(ok = tc::mbar_wait(&issued[b], k & 1, kTcWaitLimit) && tc::mbar_wait(&mmaDone[b], k & 1, kTcWaitLimit)))
                 break;
             tc::fence_after_sync();
@@ -516,10 +518,10 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
         const uint32_t id = tc::idesc(1, R);
         int issuedTiles = 0;
         for (int i = 0; i < myTiles; i++) {
-            const int b = i & 1;
-            const uint32_t k = (uint32_t)i >> 1;
+            const int b = i % W::NB;
+            const uint32_t k = (uint32_t)(i / W::NB);
             if (!(ok = tc::mbar_wait(&fullA[b], k & 1, kTcWaitLimit))) break;
-            if (i >= 2 && !(ok = tc::mbar_wait(&accFree[b], (k - 1) & 1, kTcWaitLimit))) break;
+            if (i >= W::NB && !(ok = tc::mbar_wait(&accFree[b], (k - 1) & 1, kTcWaitLimit))) break;
             tc::fence_after_sync();
             const unsigned char* sA = smem + b * kOzSlices * S::A16;
             const uint32_t dst = tmem + (uint32_t)b * W::kAccCols;
@@ -553,7 +555,7 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
     if (!ok) atomicExch(&g_tcTimeout, 1);
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_free<2 * W::kAccCols>(tmem);
+    if (warp == 0) tc::tmem_free<W::kTmemCols>(tmem);
 }
 
 // ------------------------------------------ complex128, six targets (k = 6)
@@ -1173,12 +1175,12 @@ static int dense_tc_run(State* s, const unsigned* targs, const double* g) {
         if ((rc = set_smem(kern, smem))) return rc;
         kern<<<grid, 2 * kTcThreads, smem, ctx().stream>>>((float2*)s->amps, groups, p, (const uint4*)ctx().scratch);
     } else if constexpr (KT == 3) {
-        // warp-specialised: two A buffers and two accumulator sets per CTA; shared memory
+        // warp-specialised: NB A buffers and accumulator sets per CTA; shared memory
         // padded so that no more than kMinBlocks CTAs share an SM's 512 TMEM columns
         using W = WsShape<KT>;
         const size_t perSMws = ctx().smemOptin + 1024;
         const size_t wsSmem = std::max<size_t>(
-            2 * kOzSlices * S::A16 + kOzBCopies * kOzSlices * S::B16,
+            W::NB * kOzSlices * S::A16 + kOzBCopies * kOzSlices * S::B16,
             std::min<size_t>(perSMws / (W::kMinBlocks + 1) + 1, perSMws / W::kMinBlocks - 3 * 1024));
         auto kern = k_dense_ozaki_ws<IT, KT>;
         if ((rc = set_smem(kern, wsSmem))) return rc;
