@@ -738,7 +738,7 @@ def dm_kernels_leg(dfs, circuits, small=False):
         ("oneQubitDepolarising", "k_quad<Depol1Op>", 2 * N * B, lambda: dfs.distributed_densitymatrix_oneQubitDepolarising(rho, 5, p)),
         ("twoQubitDepolarising", "k_depol2", 2 * N * B, lambda: dfs.distributed_densitymatrix_twoQubitDepolarising(rho, 1, 11, p)),
         ("damping", "k_quad<DampingOp>", 2 * N * B, lambda: dfs.distributed_densitymatrix_damping(rho, 7, p)),
-        ("manyTargGate k=1", "superoperator on 2 targets (k_many_targ_reg)", 2 * N * B,
+        ("manyTargGate k=1", "superoperator on 2 targets (tensor cores, as S (x) I on 3)", 2 * N * B,
          lambda: dfs.distributed_densitymatrix_manyTargGate(rho, [4], u1)),
         ("manyTargGate k=2", "superoperator on 4 targets (tensor cores)", 2 * N * B,
          lambda: dfs.distributed_densitymatrix_manyTargGate(rho, [2, 10], u2)),

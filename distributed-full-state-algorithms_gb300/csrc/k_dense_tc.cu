@@ -335,16 +335,16 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
 
 // ------------------------------------------ complex128, warp-specialised (k = 3)
 // The same arithmetic as k_dense_ozaki, with the phases of consecutive tiles overlapped
-// instead of separated by CTA barriers: slicer warps fill one of two shared-memory A
-// buffers, one thread issues the MMAs of a full buffer into one of two TMEM accumulator
-// sets, and epilogue warps drain the other set.  The SPR slicer threads of a group are
+// instead of separated by CTA barriers: slicer warps fill one of NB shared-memory A
+// buffers, one thread issues the MMAs of a full buffer into one of NB TMEM accumulator
+// sets, and epilogue warps drain the sets filled before it.  The SPR slicer threads of a group are
 // adjacent lanes, so the group's exponent is a shuffle away; each slices 4 amplitudes
 // (one 16-byte core row per slice).  Per buffer b, mbarriers carry the hand-offs:
 //   fullA[b]   slicers -> MMA issuer   (A[b] written, one arrival per slicer thread)
 //   issued[b]  MMA issuer -> epilogue  (MMAs issued; carries the slicers' exponents)
 //   mmaDone[b] tensor cores -> epilogue (tcgen05.commit)
 //   accFree[b] epilogue -> slicers, MMA issuer (accumulators read, so A[b] is free too)
-// Tile i uses buffer i & 1 for the (i >> 1)-th time; every wait names the parity of the
+// Tile i uses buffer i % NB for the (i / NB)-th time; every wait names the parity of the
 // phase it needs, and no barrier can run two phases ahead of a waiter (each next phase
 // depends on that waiter's own later arrival).  Every wait is bounded.
 // Shapes per target count: SPR slicer threads per group (4 amplitudes each), EPQ epilogue
