@@ -445,15 +445,24 @@ def gpu_arm(args, world, rank, local):
         ptr = C.c_void_p(hosts[0].data_ptr())
         barrier()
         t0 = time.perf_counter()
+        phases = []  # per step: upload, circuit, download (each call ends synchronised)
         for _ in range(e2e_steps):
+            ta = time.perf_counter()
             assert lib.dfs_state_set_raw(psi.handle, ptr, 0, num_amps) == 0
+            tb = time.perf_counter()
             circuits.apply(dfs, psi, gates)
+            dfs.comm_synch()
+            tc = time.perf_counter()
             assert lib.dfs_state_get_raw(psi.handle, ptr, 0, num_amps) == 0
+            phases.append((tb - ta, tc - tb, time.perf_counter() - tc))
         barrier()
         blocking_s = time.perf_counter() - t0
         per_step = {"h2d_bytes_per_step": num_amps * elem, "d2h_bytes_per_step": num_amps * elem}
+        med = [statistics.median(ph[j] for ph in phases) for j in range(3)]
         blocking = {"value": world * len(gates) * e2e_steps / blocking_s, "unit": "gates/s", **per_step,
-                    "mode": "upload, circuit, download in turn"}
+                    "mode": "upload, circuit, download in turn",
+                    "median_s": {"upload": med[0], "circuit": med[1], "download": med[2]},
+                    "host_link_gbs": {"h2d": num_amps * elem / med[0] / 1e9, "d2h": num_amps * elem / med[2] / 1e9}}
         if serving:
             # the same as a serving loop: the transfers go on the engine's copy stream
             # (dfs_state_set_raw_async / get_raw_async), so step i+1's upload and step i-1's
@@ -638,6 +647,39 @@ def batch_leg(dfs, circuits, small=False):
     return out
 
 
+def dense_kernels(dfs, circuits, psi, n):
+    """Each complex128 dense gate size alone on an n-qubit state: CUDA-event ms on the engine
+    stream (best of 3), algorithmic GB/s (the state read and written once) and fraction of
+    the measured copy bandwidth, with the tensor-pipe and ALU-pipe shares of its kernel
+    from the one-kernel ncu capture in profiles/dense_tensor_pipe.json."""
+    import torch
+    peak, peak_kind = measured_peak()
+    try:
+        prof = json.loads((ROOT / "profiles" / "dense_tensor_pipe.json").read_text())["kernels"]
+    except (OSError, KeyError, ValueError):
+        prof = {}
+    rng = np.random.default_rng(11)
+    stream = torch.cuda.current_stream()
+    out = {"qubits": n, "peak_gbs": peak, "peak_kind": peak_kind}
+    for k in (2, 3, 4, 5, 6):
+        targets = [int(t) for t in rng.choice(n, size=k, replace=False)]
+        u = circuits.haar_unitary(rng, 1 << k)
+        dfs.distributed_statevector_manyTargGate(psi, targets, u)
+        best = None
+        for _ in range(3):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            dfs.distributed_statevector_manyTargGate(psi, targets, u)
+            b.record(stream)
+            b.synchronize()
+            best = a.elapsed_time(b) if best is None else min(best, a.elapsed_time(b))
+        gbs = 2 * (1 << n) * 16 / (best * 1e-3) / 1e9
+        entry = {"targets": targets, "ms": best, "gbs": gbs, "frac": gbs / peak}
+        entry.update(prof.get(str(k), {}))
+        out[f"k{k}"] = entry
+    return out
+
+
 def precision_leg(dfs, circuits, small=False):
     """complex64 against complex128 at 32 qubits: time, <H> error and fidelity; the
     complex128 engine (parity-pinned to the oracle) stands for the FP64 reference."""
@@ -657,6 +699,7 @@ def precision_leg(dfs, circuits, small=False):
     conv.copyFrom(states["c64"])
     ip = dfs.inner_product(states["c128"], conv)
     fid = abs(ip) ** 2 / (dfs.norm_squared(states["c128"]) * dfs.norm_squared(conv))
+    res["dense_c128"] = dense_kernels(dfs, circuits, states["c128"], n)
     for s0 in list(states.values()) + [conv]:
         s0.free()
     res["c64_speedup"] = res["c64"]["gates_per_s"] / res["c128"]["gates_per_s"]

@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
     if (warp == 0) tc::tmem_free<S::COLS64>(tmem);
 }
 
-// ------------------------------------------ complex128, warp-specialised (k = 3)
+// ------------------------------------------ complex128, warp-specialised (k = 3, 4)
 // The same arithmetic as k_dense_ozaki, with the phases of consecutive tiles overlapped
 // instead of separated by CTA barriers: slicer warps fill one of NB shared-memory A
 // buffers, one thread issues the MMAs of a full buffer into one of NB TMEM accumulator
@@ -348,9 +348,10 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
 // phase it needs, and no barrier can run two phases ahead of a waiter (each next phase
 // depends on that waiter's own later arrival).  Every wait is bounded.
 // Shapes per target count: SPR slicer threads per group (4 amplitudes each), EPQ epilogue
-// warps per TMEM lane quadrant, the columns of one accumulator set, CTAs per SM.  Only
-// k = 3 uses it: at k = 4 (SPR 4, EPQ 2, one CTA per SM for the 512 TMEM columns of two
-// accumulator sets) it measured 11.8 ms at 30 qubits against 9.9 for k_dense_ozaki.
+// warps per TMEM lane quadrant, the columns of one accumulator set, CTAs per SM.  At
+// k = 4 one CTA holds an SM (three 160-column sets in 512 TMEM columns, 168 KB of shared
+// memory): 7.7 ms per 30-qubit gate against 8.7 for k_dense_ozaki (with two stages it
+// was slower, 11.8 against 9.9); k = 5 would have room for two sets only.
 template <int KT>
 struct WsShape;
 template <>
@@ -359,6 +360,13 @@ struct WsShape<3> {
     static constexpr int NB = 3;                 // pipeline depth: A buffers and accumulator sets
     static constexpr uint32_t kAccCols = 80;     // one accumulator set: 5 x 16 columns
     static constexpr uint32_t kTmemCols = 256;   // NB sets, rounded up to a power of two
+};
+template <>
+struct WsShape<4> {
+    static constexpr int SPR = 4, EPQ = 2, kMinBlocks = 1;
+    static constexpr int NB = 3;
+    static constexpr uint32_t kAccCols = 160;
+    static constexpr uint32_t kTmemCols = 512;
 };
 template <int KT>
 constexpr int ws_threads() {
@@ -1174,7 +1182,7 @@ static int dense_tc_run(State* s, const unsigned* targs, const double* g) {
         auto kern = k_dense_3xtf32<IT, KT>;
         if ((rc = set_smem(kern, smem))) return rc;
         kern<<<grid, 2 * kTcThreads, smem, ctx().stream>>>((float2*)s->amps, groups, p, (const uint4*)ctx().scratch);
-    } else if constexpr (KT == 3) {
+    } else if constexpr (KT == 3 || KT == 4) {
         // warp-specialised: NB A buffers and accumulator sets per CTA; shared memory
         // padded so that no more than kMinBlocks CTAs share an SM's 512 TMEM columns
         using W = WsShape<KT>;

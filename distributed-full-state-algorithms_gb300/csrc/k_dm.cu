@@ -175,40 +175,42 @@ struct RunDmDiagPhase {
 
 // ket gadget exp(i theta P) and bra gadget exp(i theta' P) (theta' = theta for an odd
 // number of Ys, else -theta, the reference's choice) on a string with an X or Y, on quads
-// (j, j^Xk, j^Xb, j^Xk^Xb): the ket gadget c + i s P_k, then the bra gadget c + i s' P_b,
-// both in registers, (P x)[j] = i^{#Y} (-1)^{parity((j ^ X) & YZ)} x[j ^ X] on each side.
-// (Factored, 3 complex products per amplitude; the expanded product c^2 + i c s P_k +
-// i c s' P_b - s s' P_k P_b takes 3.5.)
+// (j, j^Xk, j^Xb, j^Xk^Xb), (P x)[j] = i^{#Y} (-1)^{parity((j ^ X) & YZ)} x[j ^ X] on each
+// side.  The two gadgets commute and their product is expanded,
+//   (c + kK P_k)(c + kB P_b) = c^2 + c kK P_k + c kB P_b + kK kB P_k P_b,
+// with kK = i^m s, kB = i^m s' (m = #Y + 1), so every coefficient is real times a power
+// of i: each term is a real product of a rotated amplitude (rot: a re/im select and sign
+// flips), 8 real products per amplitude against 12 for the ket and bra gadgets in turn,
+// and one rounding instead of two.  kOdd = m odd (the re/im swap) is a template
+// parameter, so only the signs are chosen at run time.
 template <class P, class IT>
 struct DmGadgetOp {
-    typename P::R c;
-    typename P::K kK[2], kB[2];  // i s i^{#Y} (ket), i s' i^{#Y} (bra), and their negations
+    typename P::R c2, cK, cB, kk;  // c^2, c s, c s', s s'
     IT xk, xb, yzk, yzb;
     int topK, topB;  // highest X bit of each side (topK < topB)
+    int mh;          // bit 1 of m: the sign of i^m beyond its re/im swap
 };
 
-template <class P, class IT>
+template <class P, class IT, bool kOdd>
 __global__ void __launch_bounds__(kThreads) k_dm_gadget(typename P::store* __restrict__ a, IT items,
                                                         DmGadgetOp<P, IT> op) {
     const IT stride = (IT)gridDim.x * kThreads;
     for (IT j = (IT)blockIdx.x * kThreads + threadIdx.x; j < items; j += stride) {
         const IT b = insert_zero(insert_zero(j, op.topK), op.topB);
         const IT idx[4] = {b, b ^ op.xk, b ^ op.xb, b ^ op.xk ^ op.xb};
-        typename P::V x[4], y[4];
+        typename P::V x[4];
 #pragma unroll
         for (int e = 0; e < 4; e++) x[e] = P::load(a, idx[e]);
-        // the ket gadget, then the bra gadget, in registers: c x + (i s i^{#Y} sign) partner,
-        // the sign that of the partner's index (parity((i ^ X) & YZ) on each side)
 #pragma unroll
         for (int e = 0; e < 4; e++) {
-            typename P::A acc = P::first_r(op.c, x[e]);
-            P::mac(acc, parity(idx[e ^ 1] & op.yzk) ? op.kK[1] : op.kK[0], x[e ^ 1]);
-            y[e] = P::get(acc);
-        }
-#pragma unroll
-        for (int e = 0; e < 4; e++) {
-            typename P::A acc = P::first_r(op.c, y[e]);
-            P::mac(acc, parity(idx[e ^ 2] & op.yzb) ? op.kB[1] : op.kB[0], y[e ^ 2]);
+            // the ket sign of the partner x[e ^ 1], the bra sign of x[e ^ 2], and the ket
+            // sign of x[e ^ 3] inside the bra partner; i^{2m} = (-1)^m on the last term
+            const int sK1 = parity(idx[e ^ 1] & op.yzk), sB2 = parity(idx[e ^ 2] & op.yzb);
+            const int sK3 = parity(idx[e ^ 3] & op.yzk);
+            typename P::A acc = P::first_r(op.c2, x[e]);
+            P::mac_r(acc, op.cK, rot<P>(x[e ^ 1], kOdd ? 1 : 0, sK1 ^ op.mh));
+            P::mac_r(acc, op.cB, rot<P>(x[e ^ 2], kOdd ? 1 : 0, sB2 ^ op.mh));
+            P::mac_r(acc, op.kk, rot<P>(x[e ^ 3], 0, sB2 ^ sK3 ^ (kOdd ? 1 : 0)));
             P::save(a, idx[e], P::get(acc));
         }
     }
@@ -220,29 +222,23 @@ struct RunDmGadget {
         const unsigned n = s->numQubits;
         const double th2 = (numY & 1) ? theta : -theta;
         const double c = std::cos(theta), sn = std::sin(theta), sn2 = std::sin(th2);
-        // i^k times a real r, as (re, im)
-        auto ipow = [](int k, double r, double* re, double* im) {
-            const double tr[4] = {1, 0, -1, 0}, ti[4] = {0, 1, 0, -1};
-            *re = r * tr[k & 3];
-            *im = r * ti[k & 3];
-        };
+        const int m = (numY + 1) & 3;
         DmGadgetOp<P, IT> op;
-        op.c = P::mkr(c);
-        double re, im;
-        ipow(numY + 1, sn, &re, &im);
-        op.kK[0] = P::mk(re, im);
-        op.kK[1] = P::mk(-re, -im);
-        ipow(numY + 1, sn2, &re, &im);
-        op.kB[0] = P::mk(re, im);
-        op.kB[1] = P::mk(-re, -im);
+        op.c2 = P::mkr(c * c);
+        op.cK = P::mkr(c * sn);
+        op.cB = P::mkr(c * sn2);
+        op.kk = P::mkr(sn * sn2);
         op.xk = (IT)xk;
         op.xb = (IT)(xk << n);
         op.yzk = (IT)yzk;
         op.yzb = (IT)(yzk << n);
         op.topK = 63 - __builtin_clzll(xk);
         op.topB = op.topK + (int)n;
+        op.mh = (m >> 1) & 1;
         IT items = (IT)(s->numAmps / 4);
-        return launch(k_dm_gadget<P, IT>, items, 1, "pauliGadget", (typename P::store*)s->amps, items, op);
+        if (m & 1)
+            return launch(k_dm_gadget<P, IT, true>, items, 1, "pauliGadget", (typename P::store*)s->amps, items, op);
+        return launch(k_dm_gadget<P, IT, false>, items, 1, "pauliGadget", (typename P::store*)s->amps, items, op);
     }
 };
 
