@@ -351,7 +351,9 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
 // warps per TMEM lane quadrant, the columns of one accumulator set, CTAs per SM.  At
 // k = 4 one CTA holds an SM (three 160-column sets in 512 TMEM columns, 168 KB of shared
 // memory): 7.7 ms per 30-qubit gate against 8.7 for k_dense_ozaki (with two stages it
-// was slower, 11.8 against 9.9); k = 5 would have room for two sets only.
+// was slower, 11.8 against 9.9); k = 5 would have room for two sets only.  Staging the
+// slicers' loads through shared memory (a per-thread ring of cp.async copies, one or two
+// tiles ahead) instead of registers measured slower: 8.3 against 7.1 ms at k = 3.
 template <int KT>
 struct WsShape;
 template <>
@@ -1182,9 +1184,11 @@ static int dense_tc_run(State* s, const unsigned* targs, const double* g) {
         auto kern = k_dense_3xtf32<IT, KT>;
         if ((rc = set_smem(kern, smem))) return rc;
         kern<<<grid, 2 * kTcThreads, smem, ctx().stream>>>((float2*)s->amps, groups, p, (const uint4*)ctx().scratch);
-    } else if constexpr (KT == 3 || KT == 4) {
+    } else if constexpr (KT == 3 || (KT == 4 && sizeof(IT) == 4)) {
         // warp-specialised: NB A buffers and accumulator sets per CTA; shared memory
-        // padded so that no more than kMinBlocks CTAs share an SM's 512 TMEM columns
+        // padded so that no more than kMinBlocks CTAs share an SM's 512 TMEM columns.
+        // k = 4 with 64-bit indices (over 2^31 amplitudes) stays on k_dense_ozaki: 35.7
+        // against 40.4 ms at 32 qubits
         using W = WsShape<KT>;
         const size_t perSMws = ctx().smemOptin + 1024;
         const size_t wsSmem = std::max<size_t>(
