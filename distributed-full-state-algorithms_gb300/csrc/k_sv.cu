@@ -452,12 +452,12 @@ struct RunManyTarg {
     static int run(State* s, const unsigned* targs, unsigned k, const double* g) {
         if (dense_tc_supported(s, k)) return dense_tc(s, targs, k, g);
         if (k == 2 && s->vecQubits >= 3 && dense_tc_supported(s, 3)) {
-            // a two-target gate as G (x) I on a third qubit (the lowest free one): the
-            // 3-target tensor-core kernel beats double-float on the CUDA cores here (7.5
-            // against 8.9 ms at 30 qubits), and density-matrix one-target unitaries (a
-            // 4 x 4 superoperator) take the same path
-            unsigned e = 0;
-            while (e == targs[0] || e == targs[1]) e++;
+            // a two-target gate as G (x) I on a third qubit (the highest free one: a low
+            // target costs the kernel coalescing): the 3-target tensor-core kernel beats
+            // double-float on the CUDA cores here (7.1 against 8.9 ms at 30 qubits), and
+            // density-matrix one-target unitaries (a 4 x 4 superoperator) take the same path
+            unsigned e = s->vecQubits - 1;
+            while (e == targs[0] || e == targs[1]) e--;
             const unsigned t3[3] = {targs[0], targs[1], e};
             double g3[2 * 64] = {};
             for (int r = 0; r < 8; r++)
