@@ -889,17 +889,17 @@ def dm_leg(dfs, circuits, small=False):
 
 def cpu_baseline(args, circuits, gates):
     """The reference's CPU code (oracle/_ref) on the host cores: the same circuit on the
-    same-size state, timed on the stratified sample of reference_sample (two steps after
-    one warm-up step: every kind of the mix, about 10-30 s of CPU work)."""
+    same-size state, timed on the stratified sample of reference_sample (three steps after
+    one warm-up step: every kind of the mix, about 15-25 s of CPU work)."""
     try:
         kind, run_gate, free = reference_backend(circuits, args.qubits)
     except Exception as e:  # pragma: no cover
         return {"value": None, "error": str(e)}
-    value, det = reference_sample(run_gate, gates, 2, 1)
+    value, det = reference_sample(run_gate, gates, 3, 1)
     free()
     cores = os.cpu_count() or 1
     return {"value": value, "unit": "gates/s", "cores": int(os.environ.get("OMP_NUM_THREADS", cores)),
-            "kind": kind, "sample": det["sample"] + f", 2 timed steps, {args.qubits} qubits",
+            "kind": kind, "sample": det["sample"] + f", 3 timed steps, {args.qubits} qubits",
             "kind_counts": det["kind_counts"], "kind_seconds": det["kind_seconds"],
             "full_circuit_s_extrapolated": det["full_circuit_s_extrapolated"]}
 

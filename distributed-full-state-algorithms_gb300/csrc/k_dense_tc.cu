@@ -1214,8 +1214,8 @@ static int dense_tc_run(State* s, const unsigned* targs, const double* g) {
     return check_launch("manyTargGate (tensor cores)");
 }
 
-// measured at 30 qubits (ms per gate, tensor cores / CUDA cores): complex128 k = 3 7.6 /
-// 14.3, k = 4 9.0 / 46, k = 5 10.9, k = 6 18.1 / 146; complex64 k = 4 3.17 / 19, k = 5 5.05,
+// measured at 30 qubits (ms per gate, tensor cores / CUDA cores): complex128 k = 3 7.0 /
+// 14.3, k = 4 7.5 / 46, k = 5 10.5, k = 6 18.1 / 146; complex64 k = 4 3.17 / 19, k = 5 5.05,
 // k = 6 5.55, while complex64 k = 3 stays on the FP32 CUDA cores (6.0 vs 4.9 TB/s).
 bool dense_tc_supported(const State* s, unsigned k) {
     if (s->precision == DFS_C128_NATIVE || s->forceNative || !ctx().denseTensorCores) return false;
