@@ -72,6 +72,7 @@ PROTOTYPES = {
     "dfs_comm_synch": [],
     "dfs_set_stream": [_V],
     "dfs_get_stream": [_VP],
+    "dfs_set_wide_index": [_I],
     "dfs_statevector_create": [_U, _I, _HP],
     "dfs_densitymatrix_create": [_U, _I, _HP],
     "dfs_state_destroy": [_H],

@@ -24,7 +24,7 @@ from ._lib import DfsError, StateInfo, call
 
 __all__ = [
     "DfsError", "StateVector", "DensityMatrix", "comm_init", "comm_end", "comm_getRank", "comm_getNumNodes",
-    "comm_synch", "set_stream", "load", "wait_selftest",
+    "comm_synch", "set_stream", "set_wide_index", "load", "wait_selftest",
     "distributed_statevector_oneTargGate", "distributed_statevector_manyCtrlOneTargGate",
     "distributed_statevector_swapGate", "distributed_statevector_manyTargGate",
     "distributed_statevector_pauliTensor", "distributed_statevector_pauliGadget",
@@ -87,6 +87,12 @@ def set_stream(stream) -> None:
     """Issue engine work on a CUDA stream (a ``torch.cuda.Stream`` or a raw handle)."""
     handle = getattr(stream, "cuda_stream", stream)
     call("dfs_set_stream", C.c_void_p(int(handle) if handle else 0))
+
+
+def set_wide_index(on: bool) -> None:
+    """64-bit index maths for every state (``dfs_set_wide_index``), as states over 2^31
+    amplitudes take; for checking those kernels on small states."""
+    call("dfs_set_wide_index", 1 if on else 0)
 
 
 # ------------------------------------------------------------------ states

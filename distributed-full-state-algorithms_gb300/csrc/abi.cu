@@ -296,6 +296,14 @@ int dfs_set_stream(void* stream) {
     return DFS_SUCCESS;
 }
 
+int dfs_set_wide_index(int on) {
+    DFS_TRACE_CALL();
+    int rc = ensure_init();
+    if (rc) return rc;
+    g_ctx.wideIndex = on != 0;
+    return DFS_SUCCESS;
+}
+
 int dfs_get_stream(void** stream) {
     int rc = ensure_init();
     if (rc) return rc;

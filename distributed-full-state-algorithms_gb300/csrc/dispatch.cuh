@@ -8,13 +8,16 @@
 
 namespace dfs {
 
+// 64-bit index maths for states over 2^31 amplitudes (or all, dfs_set_wide_index)
+inline bool wide_index(const State* s) { return s->numAmps > (1ull << 31) || ctx().wideIndex; }
+
 // calls F::template run<P, IT>(args...) for the state's precision and size:
 // 32-bit index maths while the amplitude count fits in 31 bits.  A complex128 state
 // whose values the range guard (range.cu) has put outside the double-float window
 // runs the native FP64 instantiation on the same storage.
 template <class F, class... Args>
 int dispatch(const State* s, Args&&... args) {
-    bool wide = s->numAmps > (1ull << 31);
+    bool wide = wide_index(s);
     switch (s->precision) {
         case DFS_C128:
             if (s->forceNative)

@@ -29,6 +29,9 @@ struct Context {
     cudaEvent_t pinnedFree = nullptr;
     // dense gates on 3-4 targets go to the tensor cores (DFS_DENSE_TC=0 disables)
     bool denseTensorCores = true;
+    // 64-bit index maths for every state, not only those over 2^31 amplitudes
+    // (dfs_set_wide_index: those kernel instantiations checked at small sizes)
+    bool wideIndex = false;
     // asynchronous host transfers (dfs_state_*_raw_async) run here, beside `stream`
     cudaStream_t copyStream = nullptr;
     cudaEvent_t computeMark = nullptr;

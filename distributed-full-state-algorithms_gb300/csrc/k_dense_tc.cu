@@ -1224,7 +1224,7 @@ bool dense_tc_supported(const State* s, unsigned k) {
 }
 
 int dense_tc(State* s, const unsigned* targs, unsigned k, const double* gate) {
-    bool wide = s->numAmps > (1ull << 31);
+    bool wide = wide_index(s);
     switch (k) {
         case 3: return wide ? dense_tc_run<uint64_t, 3>(s, targs, gate) : dense_tc_run<uint32_t, 3>(s, targs, gate);
         case 4: return wide ? dense_tc_run<uint64_t, 4>(s, targs, gate) : dense_tc_run<uint32_t, 4>(s, targs, gate);

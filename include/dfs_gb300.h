@@ -71,6 +71,12 @@ int dfs_comm_synch(void);                  /* comm_synch, src/communication.hpp:
 int dfs_set_stream(void* cuda_stream);
 int dfs_get_stream(void** cuda_stream);
 
+/* Index width of the kernels (no reference counterpart; the reference's Index is 64-bit,
+ * src/types.hpp).  By default a state of up to 2^31 amplitudes runs 32-bit index maths and
+ * a larger one 64-bit; on != 0 makes every state take the 64-bit instantiations, so that
+ * they can be checked against the oracle on small states.  Results are the same either way. */
+int dfs_set_wide_index(int on);
+
 /* ----------------------------------------------------------------- states */
 
 /* device precision of a state */

@@ -1,0 +1,50 @@
+"""The 64-bit index instantiations of every kernel, which states over 2^31 amplitudes
+take (src/types.hpp's Index is 64-bit), checked against the oracle on small states:
+dfs_set_wide_index(1) makes every state take them, and the statevector and
+density-matrix parity tests run again under it."""
+import pytest
+
+import test_dm_gpu as dm
+import test_sv_gpu as sv
+
+PRECISIONS = sv.PRECISIONS
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture
+def wide(dfs):
+    dfs.set_wide_index(True)
+    try:
+        yield
+    finally:
+        dfs.set_wide_index(False)
+
+
+SV_TESTS = [sv.test_one_targ_all_positions, sv.test_many_ctrl_one_targ, sv.test_swap, sv.test_pauli_tensor,
+            sv.test_pauli_gadget, sv.test_pauli_z_only_and_identity, sv.test_phase_gadget,
+            sv.test_many_targ_whole_register]
+DM_TESTS = [dm.test_many_targ, dm.test_swap, dm.test_pauli_tensor_and_gadget, dm.test_kraus_map, dm.test_channels,
+            dm.test_expec_pauli_string, dm.test_partial_trace, dm.test_partial_trace_many_outputs]
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+@pytest.mark.parametrize("case", SV_TESTS + DM_TESTS, ids=lambda f: f.__module__[5:] + "." + f.__name__[5:])
+def test_wide_index(dfs, oracle, prec, rng, wide, case):
+    case(dfs, oracle, prec, rng)
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5, 6])
+def test_wide_index_many_targ(dfs, oracle, prec, k, rng, wide):
+    sv.test_many_targ(dfs, oracle, prec, k, rng)
+
+
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+def test_wide_index_many_targ_6_many_tiles(dfs, oracle, prec, rng, wide):
+    sv.test_many_targ_6_many_tiles(dfs, oracle, prec, rng)
+
+
+def test_wide_index_switch_is_restored(dfs, oracle, rng):
+    # the fixture turns it off again: the default path still matches
+    sv.test_swap(dfs, oracle, "c128", rng)
