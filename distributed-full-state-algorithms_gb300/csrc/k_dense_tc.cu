@@ -416,7 +416,8 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
         //      two parts of a row fell in the same banks), and the row's parts are lanes
         //      8 apart.  k = 3: 7.10 -> 6.97 ms at 30 qubits; k = 4: 7.75 -> 7.51
         constexpr int H = 4;
-        constexpr int kLgSPR = W::SPR == 1 ? 0 : (W::SPR == 2 ? 1 : (W::SPR == 4 ? 2 : 3));
+        static_assert(W::SPR == 2 || W::SPR == 4, "a warp holds 8-row blocks of whole groups");
+        constexpr int kLgSPR = W::SPR == 2 ? 1 : 2;
         const int row = warp * (32 / W::SPR) + (lane & 7) + ((lane >> (3 + kLgSPR)) << 3);
         const int part = (lane >> 3) & (W::SPR - 1);
         auto load = [&](int i, uint4 (&v)[H]) {
