@@ -532,11 +532,13 @@ DEV typename P::V sum_value(const typename SumOf<P>::T& s) {
 
 // many outputs (4^(n-k) >= 2^20): each thread sums kPtPer outputs at a time, the loads of
 // all of them issued for each traced index before they are added (memory-level parallelism);
-// the traced offsets sel[] sit in shared memory when they fit
-constexpr int kPtPer = 4;
+// the traced offsets sel[] sit in shared memory when they fit.  kPer outputs per thread:
+// one while each output sums at most 4 traced terms (full occupancy hides the latency:
+// a 15-qubit matrix traced over one qubit in 1.98 ms against 2.87 with four outputs per
+// thread), two beyond (3 qubits: 0.66 against 0.75 ms with four, 0.69 with one)
 constexpr int kPtSmemSel = 1024;
 
-template <class P, class IT>
+template <class P, class IT, int kPtPer>
 __global__ void __launch_bounds__(kThreads) k_partial_trace(const typename P::store* __restrict__ in,
                                                             typename P::store* __restrict__ out, IT numOut, QList all,
                                                             const uint64_t* __restrict__ sel, int k) {
@@ -617,10 +619,11 @@ struct RunPartialTrace {
         if (rc) return rc;
         IT numOut = (IT)out->numAmps;
         if ((uint64_t)numOut >= (1ull << 20)) {
-            Launch L = launch_for(numOut, kPtPer, ctx().numSMs, 16);
-            k_partial_trace<P, IT><<<L.grid, L.block, 0, ctx().stream>>>((const typename P::store*)in->amps,
-                                                                           (typename P::store*)out->amps, numOut, q,
-                                                                           (const uint64_t*)ctx().scratch, (int)k);
+            const bool one = k <= 2;
+            Launch L = launch_for(numOut, one ? 1 : 2, ctx().numSMs, 16);
+            auto kern = one ? k_partial_trace<P, IT, 1> : k_partial_trace<P, IT, 2>;
+            kern<<<L.grid, L.block, 0, ctx().stream>>>((const typename P::store*)in->amps, (typename P::store*)out->amps,
+                                                       numOut, q, (const uint64_t*)ctx().scratch, (int)k);
         } else {
             Launch L = launch_for((uint64_t)numOut * 32, 1, ctx().numSMs, 16);
             k_partial_trace_warp<P, IT><<<L.grid, L.block, 0, ctx().stream>>>(

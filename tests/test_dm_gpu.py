@@ -151,6 +151,21 @@ def test_partial_trace_many_outputs(dfs, oracle, prec, rng):
         assert rel_err(into.getAllVecAmps(), oracle.dm_partial_trace(a, t)) <= TOL[prec]
 
 
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_partial_trace_many_outputs_three_qubits(dfs, oracle, prec, rng):
+    """13 qubits with three traced qubits: 4^10 outputs of 8 traced terms each, the kernel's
+    form with two outputs per thread (one or two traced qubits take one per thread)."""
+    n = 13
+    a = gaussian_state(rng, 1 << (2 * n))
+    rho = dfs.DensityMatrix(n, precision=prec)
+    rho.setAmps(a)
+    a = rho.getAllVecAmps()
+    for t in ([0, 6, 12], [2, 7, 11]):
+        out = dfs.distributed_densitymatrix_partialTrace(rho, t)
+        assert rel_err(out.getAllVecAmps(), oracle.dm_partial_trace(a, t)) <= TOL[prec]
+        out.free()
+
+
 def test_trace_and_matrix_view(dfs, rng):
     n = 4
     m = gaussian_matrix(rng, 1 << n)
