@@ -1,11 +1,13 @@
 """The 64-bit index instantiations of every kernel, which states over 2^31 amplitudes
 take (src/types.hpp's Index is 64-bit), checked against the oracle on small states:
-dfs_set_wide_index(1) makes every state take them, and the statevector and
-density-matrix parity tests run again under it."""
+dfs_set_wide_index(1) makes every state take them, and the statevector, density-matrix,
+reduction, adjoint-gradient and allocation-free parity tests run again under it."""
 import pytest
 
+import test_adjoint_gpu as adj
 import test_dm_gpu as dm
 import test_sv_gpu as sv
+import test_zz_no_alloc as noalloc
 
 PRECISIONS = sv.PRECISIONS
 
@@ -43,6 +45,23 @@ def test_wide_index_many_targ(dfs, oracle, prec, k, rng, wide):
 @pytest.mark.parametrize("prec", ["c128", "c64"])
 def test_wide_index_many_targ_6_many_tiles(dfs, oracle, prec, rng, wide):
     sv.test_many_targ_6_many_tiles(dfs, oracle, prec, rng)
+
+
+def test_wide_index_reductions(dfs, oracle, rng, wide):
+    sv.test_reductions_sv(dfs, oracle, rng)
+
+
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+@pytest.mark.parametrize("case", [adj.test_statevector_gadget_ansatz, adj.test_statevector_gate_mix,
+                                  adj.test_density_matrix_channels_and_gadgets],
+                         ids=lambda f: f.__name__[5:])
+def test_wide_index_adjoint(dfs, oracle, prec, rng, wide, case):
+    case(dfs, oracle, prec, rng)
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_wide_index_noalloc(dfs, prec, wide):
+    noalloc.test_noalloc_matches_expecPauliString_twice(dfs, prec)
 
 
 def test_wide_index_switch_is_restored(dfs, oracle, rng):
