@@ -347,7 +347,9 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
 //   accFree[b] epilogue -> slicers, MMA issuer (accumulators read, so A[b] is free too)
 // Tile i uses buffer i % NB for the (i / NB)-th time; every wait names the parity of the
 // phase it needs, and no barrier can run two phases ahead of a waiter (each next phase
-// depends on that waiter's own later arrival).  Every wait is bounded.
+// depends on that waiter's own later arrival).  Every wait is bounded, and a slicer or
+// epilogue warp gives up as a whole (a vote over its lanes): its shuffles and
+// tcgen05.ld.sync.aligned need every lane.
 // Shapes per target count: SPR slicer threads per group (4 amplitudes each), EPQ epilogue
 // warps per TMEM lane quadrant, the columns of one accumulator set, CTAs per SM.  At
 // k = 4 one CTA holds an SM (three 160-column sets in 512 TMEM columns, 168 KB of shared
@@ -433,7 +435,7 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
         for (int i = 0; i < myTiles; i++) {
             const int b = i % W::NB;
             const uint32_t k = (uint32_t)(i / W::NB);
-            if (i >= W::NB && !(ok = tc::mbar_wait(&accFree[b], (k - 1) & 1, kTcWaitLimit))) break;
+            if (i >= W::NB && !(ok = __all_sync(0xffffffffu, tc::mbar_wait(&accFree[b], (k - 1) & 1, kTcWaitLimit)))) break;
             uint32_t E32 = 0;
 #pragma unroll
             for (int c = 0; c < H; c++) E32 = max(E32, max(exp_field(cur[c].y), exp_field(cur[c].w)));
@@ -491,7 +493,8 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
         for (int i = 0; i < myTiles; i++) {
             const int b = i % W::NB;
             const uint32_t k = (uint32_t)(i / W::NB);
-            if (!(ok = tc::mbar_wait(&issued[b], k & 1, kTcWaitLimit) && tc::mbar_wait(&mmaDone[b], k & 1, kTcWaitLimit)))
+            if (!(ok = __all_sync(0xffffffffu, tc::mbar_wait(&issued[b], k & 1, kTcWaitLimit) &&
+                                                   tc::mbar_wait(&mmaDone[b], k & 1, kTcWaitLimit))))
                 break;
             tc::fence_after_sync();
             const uint32_t E = sE[b][row];
@@ -701,7 +704,7 @@ __global__ void __launch_bounds__(kOz6Threads, 1)
             const int b = i & 1;
             const uint32_t k = (uint32_t)i >> 1;
             load(i + 1, nxt, nxtBase);
-            if (i >= 2 && !(ok = tc::mbar_wait(&accFree[b], (k - 1) & 1, kTcWaitLimit))) break;
+            if (i >= 2 && !(ok = __all_sync(0xffffffffu, tc::mbar_wait(&accFree[b], (k - 1) & 1, kTcWaitLimit)))) break;
             uint32_t E = 0;
 #pragma unroll
             for (int c = 0; c < H; c++) E = max(E, max((cur[c].y >> 20) & 0x7FFu, (cur[c].w >> 20) & 0x7FFu));
@@ -770,7 +773,8 @@ __global__ void __launch_bounds__(kOz6Threads, 1)
         for (int i = 0; i < myTiles; i++) {
             const int b = i & 1;
             const uint32_t k = (uint32_t)i >> 1;
-            if (!(ok = tc::mbar_wait(&issued[b], k & 1, kTcWaitLimit) && tc::mbar_wait(&mmaDone[b], k & 1, kTcWaitLimit)))
+            if (!(ok = __all_sync(0xffffffffu, tc::mbar_wait(&issued[b], k & 1, kTcWaitLimit) &&
+                                                   tc::mbar_wait(&mmaDone[b], k & 1, kTcWaitLimit))))
                 break;
             tc::fence_after_sync();
             const IT gt = ((IT)blockIdx.x + (IT)i * gridDim.x) * kOz6Groups;
