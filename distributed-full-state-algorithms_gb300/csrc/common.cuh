@@ -43,6 +43,19 @@ DEV IT insert_zeros(IT j, const QList& q) {
     return j;
 }
 
+// the same for a list whose length N is known at compile time: unrolled, no loop
+// overhead or parameter-indexing latency per qubit (the controlled gate's 3-qubit
+// deposit in a loop cost its sweep ~10% against the one-target gate's)
+template <int N, class IT>
+DEV IT insert_zeros_n(IT j, const QList& q) {
+#pragma unroll
+    for (int s = 0; s < N; s++) {
+        const IT low = (IT)q.low[s];
+        j = ((j & ~low) << 1) | (j & low);
+    }
+    return j;
+}
+
 template <typename IT>
 DEV IT insert_zero(IT j, int q) {
     IT low = (((IT)1) << q) - 1;

@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
     auto load = [&](IT tile, uint4 (&v)[kHalf]) {
         const IT g = tile * 128 + (IT)row;
         const bool ok = tile < numTiles && g < numGroups;
-        const IT b = ok ? insert_zeros(g, p.q) : (IT)0;
+        const IT b = ok ? insert_zeros_n<KT>(g, p.q) : (IT)0;
 #pragma unroll
         for (int c = 0; c < kHalf; c++) v[c] = ok ? amps[b + p.off[half * kHalf + c]] : make_uint4(0, 0, 0, 0);
     };
@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(2 * kTcThreads, KT == 3 ? 4 : (KT == 4 ? 2 : 1
     for (IT tile = blockIdx.x; tile < numTiles; tile += gridDim.x) {
         const IT g = tile * 128 + (IT)row;
         const bool valid = g < numGroups;
-        const IT base = valid ? insert_zeros(g, p.q) : (IT)0;
+        const IT base = valid ? insert_zeros_n<KT>(g, p.q) : (IT)0;
 
         // ---- the group's largest exponent (both halves)
         uint32_t E32 = 0;
@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
         auto load = [&](int i, uint4 (&v)[H]) {
             const IT g = ((IT)blockIdx.x + (IT)i * gridDim.x) * 128 + (IT)row;
             const bool in = i < myTiles && g < numGroups;
-            const IT b = in ? insert_zeros(g, p.q) : (IT)0;
+            const IT b = in ? insert_zeros_n<KT>(g, p.q) : (IT)0;
 #pragma unroll
             for (int c = 0; c < H; c++) v[c] = in ? amps[b + p.off[part * H + c]] : make_uint4(0, 0, 0, 0);
         };
@@ -500,7 +500,7 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
             const uint32_t E = sE[b][row];
             const IT g = ((IT)blockIdx.x + (IT)i * gridDim.x) * 128 + (IT)row;
             const bool valid = g < numGroups;
-            const IT base = valid ? insert_zeros(g, p.q) : (IT)0;
+            const IT base = valid ? insert_zeros_n<KT>(g, p.q) : (IT)0;
             const uint32_t lanes = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)b * W::kAccCols;
             const uint32_t rowc = (uint32_t)((int)E + 896 - kOzShift) << 20;
             // the whole warp's results are normal doubles (the usual case) or it takes the
@@ -920,7 +920,7 @@ __global__ void __launch_bounds__(2 * kTcThreads) k_dense_3xtf32(float2* __restr
     for (IT tile = blockIdx.x; tile < numTiles && !timedOut; tile += gridDim.x) {
         const IT g = tile * 128 + (IT)row;
         const bool valid = g < numGroups;
-        const IT base = valid ? insert_zeros(g, p.q) : (IT)0;
+        const IT base = valid ? insert_zeros_n<KT>(g, p.q) : (IT)0;
         float2 xv[DH];  // this thread's amplitudes of the chunk; reals [re x0, im x0, re x1, ...]
 #pragma unroll
         for (int c = 0; c < DH; c++) xv[c] = valid ? amps[base + p.off[half * DH + c]] : make_float2(0.f, 0.f);

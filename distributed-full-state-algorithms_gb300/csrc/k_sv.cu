@@ -51,14 +51,16 @@ int sv_one_targ(State* s, unsigned t, const double* gate) { return dispatch<RunO
 // ------------------------------------------------ many controls, one target
 // local_statevector_manyCtrlOneTargGate, src/local_statevector.hpp:32-51
 
-template <class P, class IT>
+// N: the number of controls and target when it is 2..4 (an unrolled deposit), else 0
+template <class P, class IT, int N = 0>
 struct CtrlOneTargOp {
     typename P::K g[4];
     QList q;        // controls and target, sorted
     IT setMask;     // all control bits and the target bit
     IT tbit;
     DEV void index(IT j, IT& i0, IT& i1) const {
-        i1 = insert_zeros(j, q) | setMask;
+        if constexpr (N > 0) i1 = insert_zeros_n<N>(j, q) | setMask;
+        else i1 = insert_zeros(j, q) | setMask;
         i0 = i1 ^ tbit;
     }
     DEV void apply(IT, IT, typename P::V& x0, typename P::V& x1) const {
@@ -72,9 +74,9 @@ struct CtrlOneTargOp {
 };
 
 struct RunCtrlOneTarg {
-    template <class P, class IT>
-    static int run(State* s, const unsigned* ctrls, unsigned nc, unsigned t, const double* g) {
-        CtrlOneTargOp<P, IT> op;
+    template <class P, class IT, int N>
+    static int go(State* s, const unsigned* ctrls, unsigned nc, unsigned t, const double* g) {
+        CtrlOneTargOp<P, IT, N> op;
         std::vector<unsigned> qs(ctrls, ctrls + nc);
         qs.push_back(t);
         op.q = make_qlist(qs);
@@ -84,8 +86,17 @@ struct RunCtrlOneTarg {
         op.tbit = (IT)(1ull << t);
         for (int i = 0; i < 4; i++) op.g[i] = P::mk(g[2 * i], g[2 * i + 1]);
         IT items = (IT)(s->numAmps >> (nc + 1));
-        return launch(k_pair<P, IT, CtrlOneTargOp<P, IT>>, items, pair_per<P>(), "manyCtrlOneTargGate",
+        return launch(k_pair<P, IT, CtrlOneTargOp<P, IT, N>>, items, pair_per<P>(), "manyCtrlOneTargGate",
                       (typename P::store*)s->amps, items, op);
+    }
+    template <class P, class IT>
+    static int run(State* s, const unsigned* ctrls, unsigned nc, unsigned t, const double* g) {
+        switch (nc) {
+            case 1: return go<P, IT, 2>(s, ctrls, nc, t, g);
+            case 2: return go<P, IT, 3>(s, ctrls, nc, t, g);
+            case 3: return go<P, IT, 4>(s, ctrls, nc, t, g);
+            default: return go<P, IT, 0>(s, ctrls, nc, t, g);
+        }
     }
 };
 int sv_ctrl_one_targ(State* s, const unsigned* ctrls, unsigned nc, unsigned t, const double* gate) {
