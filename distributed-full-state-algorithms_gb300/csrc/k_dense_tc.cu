@@ -505,10 +505,11 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
             const uint32_t rowc = (uint32_t)((int)E + 896 - kOzShift) << 20;
             // the whole warp's results are normal doubles (the usual case) or it takes the
             // general encoding; one instantiation each keeps both free of the other's branches
-            auto drain_tile = [&](auto normalTag) {
+            auto drain_tile = [&](auto normalTag, auto cgTag) {
                 constexpr bool kNormal = decltype(normalTag)::value;
+                constexpr int kCg = decltype(cgTag)::value;
 #pragma unroll
-                for (int ch = cg; ch < D / 4; ch += W::EPQ) {
+                for (int ch = kCg; ch < D / 4; ch += W::EPQ) {
                     float acc[kOzAccs][8];
 #pragma unroll
                     for (int u = 0; u < kOzAccs; u++) {
@@ -543,8 +544,16 @@ __global__ void __launch_bounds__(ws_threads<KT>(), WsShape<KT>::kMinBlocks)
                     }
                 }
             };
-            if (__all_sync(0xffffffffu, (int)E >= p.fastE || !valid)) drain_tile(std::true_type{});
-            else drain_tile(std::false_type{});
+            // the first chunk index is a template constant (one instantiation per value), so
+            // the TMEM columns, output offsets and row exponents fold into constants: k = 3
+            // 6.91 -> 6.83 ms at 30 qubits, k = 4 7.45 -> 7.33
+            auto drain_chunks = [&](auto normalTag) {
+                static_assert(W::EPQ <= 2, "chunk groups 0 and 1");
+                if (W::EPQ == 1 || cg == 0) drain_tile(normalTag, std::integral_constant<int, 0>{});
+                else drain_tile(normalTag, std::integral_constant<int, 1>{});
+            };
+            if (__all_sync(0xffffffffu, (int)E >= p.fastE || !valid)) drain_chunks(std::true_type{});
+            else drain_chunks(std::false_type{});
             tc::fence_before_sync();
             tc::mbar_arrive(&accFree[b]);
         }
