@@ -32,6 +32,10 @@ unsigned adj_partial_cols();
 // partial sums of sum_j conj(ad_j) (-1)^{par((j^X)&YZ)} st_{j^X} into row[0..cols),
 // then st, ad <- exp(-i phi Q)
 int adj_gadget_step(State* st, State* ad, uint64_t maskX, uint64_t maskYZ, int numY, double phi, double2* row);
+// the same for two gadgets in one sweep over both vectors (g2 the later one, undone
+// first): g2's partial sums into row2, g1's into row1, then st, ad <- G1^dag G2^dag
+int adj_two_gadgets_step(State* st, State* ad, const GadgetSpec& g1, const GadgetSpec& g2, double2* row1,
+                         double2* row2);
 // out <- H psi; partial sums of <psi|out> into row
 int adj_pauli_sum_apply(State* psi, State* out, const AdjTerm* terms, unsigned numTerms, double2* row);
 // s <- vec(H) of a density matrix

@@ -101,6 +101,14 @@ static bool odd_y(const std::vector<unsigned>& paulis) {
     return c & 1;
 }
 
+// a statevector Pauli gadget with an X or Y as masks and angle (false for anything else)
+static bool gadget_spec(const CircOp& op, const double* params, GadgetSpec* g) {
+    if (op.kind != OP_PAULI_GADGET) return false;
+    pauli_masks(op.targs, op.paulis, 0, &g->x, &g->yz, &g->numY);
+    g->theta = op.val(params);
+    return g->x != 0;
+}
+
 // ------------------------------------------------------- operation replay
 
 // forward (adjoint = false) or adjoint (adjoint = true: U^dagger, -theta) of a
@@ -542,10 +550,19 @@ static int forward(Circuit* c, State* s, const double* params, bool keepCheckpoi
         FusedPlan* pl = c->plan;
         int rc = upload_angles(c, pl, params);
         if (rc) return rc;
-        for (const FusedSeg& seg : pl->segs) {
+        for (size_t i = 0; i < pl->segs.size(); i++) {
+            const FusedSeg& seg = pl->segs[i];
             if (!seg.fused) {
                 const CircOp& op = c->ops[seg.first];
-                rc = apply_op(s, op, op.val(params), false);
+                // two consecutive Pauli gadgets with different X parts: one sweep (k_sv.cu)
+                GadgetSpec g1, g2;
+                if (i + 1 < pl->segs.size() && !pl->segs[i + 1].fused && gadget_spec(op, params, &g1) &&
+                    gadget_spec(c->ops[pl->segs[i + 1].first], params, &g2) && g1.x != g2.x) {
+                    rc = sv_two_gadgets(s, g1, g2);
+                    i++;
+                } else {
+                    rc = apply_op(s, op, op.val(params), false);
+                }
             } else {
                 rc = fused_run(s, launch_of(pl, seg, s->numQubits));
             }
@@ -660,6 +677,22 @@ static int backward(Circuit* c, const double* params, double* grad) {
         for (size_t g = pl->segs.size(); g-- > 0;) {
             const FusedSeg& seg = pl->segs[g];
             if (!seg.fused) {
+                // two consecutive parametrised Pauli gadgets with different X parts: undone
+                // in one sweep over both vectors, each with its own row of sums
+                const CircOp& op2 = c->ops[seg.first];
+                GadgetSpec g1, g2;
+                if (g > 0 && !pl->segs[g - 1].fused && op2.param >= 0 && c->ops[pl->segs[g - 1].first].param >= 0 &&
+                    gadget_spec(op2, params, &g2) && gadget_spec(c->ops[pl->segs[g - 1].first], params, &g1) &&
+                    g1.x != g2.x) {
+                    const CircOp& op1 = c->ops[pl->segs[g - 1].first];
+                    double2* row2 = L.parts + (size_t)uses.size() * L.cols;
+                    uses.push_back({op2.param, 0, g2.numY, 2.0});
+                    double2* row1 = L.parts + (size_t)uses.size() * L.cols;
+                    uses.push_back({op1.param, 0, g1.numY, 2.0});
+                    if ((rc = adj_two_gadgets_step(st, ad, g1, g2, row1, row2))) return rc;
+                    g--;
+                    continue;
+                }
                 if ((rc = undo(seg.first))) return rc;
                 continue;
             }

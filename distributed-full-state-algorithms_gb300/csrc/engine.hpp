@@ -97,6 +97,24 @@ inline size_t elem_bytes(int precision) { return precision == DFS_C64 ? 8 : 16; 
 // All take validated arguments.  Gate matrices are row-major interleaved doubles.
 
 // k_sv.cu
+// a Pauli gadget exp(i theta P) by its masks: X = qubits with X or Y, YZ = with Y or Z
+struct GadgetSpec {
+    uint64_t x, yz;
+    int numY;
+    double theta;
+};
+// the zero bits (lo < hi) of the representatives of the quads {r, r^x1, r^x2, r^x1^x2}
+// (x1 != x2, both nonzero): the top bit of x1, and the top bit of x2 or x2 ^ x1,
+// whichever has the first bit clear
+inline void two_gadget_bits(uint64_t x1, uint64_t x2, int* lo, int* hi) {
+    const int a = 63 - __builtin_clzll(x1);
+    const uint64_t x2p = ((x2 >> a) & 1) ? x2 ^ x1 : x2;
+    const int b = 63 - __builtin_clzll(x2p);
+    *lo = a < b ? a : b;
+    *hi = a < b ? b : a;
+}
+// exp(i t2 P2) exp(i t1 P1) in one sweep; both X masks nonzero and different
+int sv_two_gadgets(State* s, const GadgetSpec& g1, const GadgetSpec& g2);
 int sv_one_targ(State* s, unsigned t, const double* gate);
 int sv_ctrl_one_targ(State* s, const unsigned* ctrls, unsigned nc, unsigned t, const double* gate);
 int sv_swap(State* s, unsigned q1, unsigned q2);

@@ -78,6 +78,85 @@ __global__ void __launch_bounds__(kThreads) k_adj_gadget_pair(typename P::store*
     if (threadIdx.x == 0) partials[blockIdx.x] = sum_to_double2(s);
 }
 
+// Two consecutive gadgets G2 G1 (X1 != X2, both nonzero) undone in one sweep over both
+// vectors, on the quads {r, r^X1, r^X2, r^X1^X2} of the forward kernel (k_sv.cu
+// k_two_gadgets): g2's sums from the vectors after G2, then both <- G2^dag in registers,
+// g1's sums, both <- G1^dag, one store.  Half the bytes of two k_adj_gadget_pair sweeps.
+template <class P, class IT>
+struct AdjTwoGadgetOp {
+    typename P::R c1, sn1, c2, sn2;  // cos and -sin of each angle (the inverse gadgets)
+    IT x1, x2, yz1, yz2;
+    int lo, hi, m1, m2;
+};
+
+template <class P, class IT>
+__global__ void __launch_bounds__(kThreads) k_adj_two_gadgets(typename P::store* __restrict__ st,
+                                                              typename P::store* __restrict__ ad, IT items,
+                                                              AdjTwoGadgetOp<P, IT> op, double2* __restrict__ parts1,
+                                                              double2* __restrict__ parts2) {
+    using Sum = typename SumOf<P>::T;
+    Sum S1, S2;
+    sum_zero(S1);
+    sum_zero(S2);
+    const IT stride = (IT)gridDim.x * kThreads;
+    for (IT j = (IT)blockIdx.x * kThreads + threadIdx.x; j < items; j += stride) {
+        const IT r = insert_zero(insert_zero(j, op.lo), op.hi);
+        const IT idx[4] = {r, r ^ op.x1, r ^ op.x2, r ^ op.x1 ^ op.x2};
+        typename P::V x[4], l[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            x[e] = P::load(st, idx[e]);
+            l[e] = P::load(ad, idx[e]);
+        }
+        int sg1[4], sg2[4];  // the sign of each element's partner under P1 and P2
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            sg1[e] = parity(idx[e ^ 1] & op.yz1);
+            sg2[e] = parity(idx[e ^ 2] & op.yz2);
+        }
+        // gadget 2: sums, then undone on both vectors (pairs e, e ^ 2)
+#pragma unroll
+        for (int e = 0; e < 4; e++) sum_add_conj_prod(S2, l[e], x[e ^ 2], sg2[e]);
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+            typename P::A a0 = P::first_r(op.c2, x[e]);
+            P::mac_r(a0, op.sn2, rot<P>(x[e ^ 2], op.m2, sg2[e]));
+            typename P::A a1 = P::first_r(op.c2, x[e ^ 2]);
+            P::mac_r(a1, op.sn2, rot<P>(x[e], op.m2, sg2[e ^ 2]));
+            x[e] = P::get(a0);
+            x[e ^ 2] = P::get(a1);
+            typename P::A b0 = P::first_r(op.c2, l[e]);
+            P::mac_r(b0, op.sn2, rot<P>(l[e ^ 2], op.m2, sg2[e]));
+            typename P::A b1 = P::first_r(op.c2, l[e ^ 2]);
+            P::mac_r(b1, op.sn2, rot<P>(l[e], op.m2, sg2[e ^ 2]));
+            l[e] = P::get(b0);
+            l[e ^ 2] = P::get(b1);
+        }
+        // gadget 1 (pairs e, e ^ 1)
+#pragma unroll
+        for (int e = 0; e < 4; e++) sum_add_conj_prod(S1, l[e], x[e ^ 1], sg1[e]);
+#pragma unroll
+        for (int e = 0; e < 4; e += 2) {
+            typename P::A a0 = P::first_r(op.c1, x[e]);
+            P::mac_r(a0, op.sn1, rot<P>(x[e ^ 1], op.m1, sg1[e]));
+            typename P::A a1 = P::first_r(op.c1, x[e ^ 1]);
+            P::mac_r(a1, op.sn1, rot<P>(x[e], op.m1, sg1[e ^ 1]));
+            P::save(st, idx[e], P::get(a0));
+            P::save(st, idx[e ^ 1], P::get(a1));
+            typename P::A b0 = P::first_r(op.c1, l[e]);
+            P::mac_r(b0, op.sn1, rot<P>(l[e ^ 1], op.m1, sg1[e]));
+            typename P::A b1 = P::first_r(op.c1, l[e ^ 1]);
+            P::mac_r(b1, op.sn1, rot<P>(l[e], op.m1, sg1[e ^ 1]));
+            P::save(ad, idx[e], P::get(b0));
+            P::save(ad, idx[e ^ 1], P::get(b1));
+        }
+    }
+    S1 = block_reduce(S1);
+    if (threadIdx.x == 0) parts1[blockIdx.x] = sum_to_double2(S1);
+    S2 = block_reduce(S2);
+    if (threadIdx.x == 0) parts2[blockIdx.x] = sum_to_double2(S2);
+}
+
 // strings without X or Y: exp(i phi Z..Z) is diagonal
 template <class P, class IT>
 __global__ void __launch_bounds__(kThreads) k_adj_gadget_diag(typename P::store* __restrict__ st,
@@ -299,6 +378,34 @@ struct RunAdjGadget {
 };
 int adj_gadget_step(State* st, State* ad, uint64_t maskX, uint64_t maskYZ, int numY, double phi, double2* row) {
     return dispatch<RunAdjGadget>(st, st, ad, maskX, maskYZ, numY, phi, row);
+}
+
+struct RunAdjTwoGadgets {
+    template <class P, class IT>
+    static int run(State* st, State* ad, const GadgetSpec& g1, const GadgetSpec& g2, double2* row1, double2* row2) {
+        using S = typename P::store;
+        AdjTwoGadgetOp<P, IT> op;
+        op.c1 = P::mkr(std::cos(g1.theta));
+        op.sn1 = P::mkr(-std::sin(g1.theta));
+        op.c2 = P::mkr(std::cos(g2.theta));
+        op.sn2 = P::mkr(-std::sin(g2.theta));
+        op.x1 = (IT)g1.x;
+        op.x2 = (IT)g2.x;
+        op.yz1 = (IT)g1.yz;
+        op.yz2 = (IT)g2.yz;
+        two_gadget_bits(g1.x, g2.x, &op.lo, &op.hi);
+        op.m1 = (g1.numY + 1) & 3;
+        op.m2 = (g2.numY + 1) & 3;
+        IT items = (IT)(st->numAmps / 4);
+        k_adj_two_gadgets<P, IT><<<adj_grid(items), kThreads, 0, ctx().stream>>>((S*)st->amps, (S*)ad->amps, items, op,
+                                                                                 row1, row2);
+        return check_launch("adjoint of two gadgets");
+    }
+};
+int adj_two_gadgets_step(State* st, State* ad, const GadgetSpec& g1, const GadgetSpec& g2, double2* row1,
+                         double2* row2) {
+    if (g1.x == 0 || g2.x == 0 || g1.x == g2.x) return fail(DFS_ERR_INVALID_ARG, "two gadgets need distinct X parts");
+    return dispatch<RunAdjTwoGadgets>(st, st, ad, g1, g2, row1, row2);
 }
 
 struct RunPauliSumApply {

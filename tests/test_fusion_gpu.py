@@ -62,3 +62,42 @@ def test_fused_gradients(dfs, rng, prec, tol):
             out[fusion] = (loss, circ.gradient(params))
         assert abs(out[True][0] - out[False][0]) <= (1e-12 if prec == "c128" else 1e-5) * np.sum(np.abs(coeffs))
         assert np.max(np.abs(out[True][1] - out[False][1])) <= tol * max(1.0, np.max(np.abs(out[False][1])))
+
+
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-10), ("c128_native", 1e-10), ("c64", 2e-4)])
+def test_paired_gadgets(dfs, oracle, prec, tol, rng):
+    """Consecutive Pauli gadgets with different X parts run two to a sweep, forward and in
+    the adjoint: against the oracle, the operation-by-operation pass and its gradients.
+    The circuit also holds pairs that run one by one (equal X parts, a Z-only string, a
+    gadget next to another kind of operation)."""
+    n = 20
+    G = circuits.Gate
+    gates = circuits.gadget_ansatz(n, layers=3, per_layer=12, seed=int(rng.integers(1 << 30)))
+    gates += [G("pauli_gadget", (2, 9), paulis=(1, 3), param=0.3), G("pauli_gadget", (2, 9), paulis=(2, 2), param=-0.7),
+              G("pauli_gadget", (4, 17), paulis=(3, 3), param=0.5), G("pauli_gadget", (19, 0), paulis=(2, 1), param=1.1),
+              G("swap", (3, 18)), G("pauli_gadget", (5, 6, 7), paulis=(1, 2, 3), param=-0.4),
+              G("pauli_gadget", (0, 19), paulis=(1, 1), param=0.9), G("pauli_gadget", (0, 19), paulis=(2, 1), param=0.2)]
+    coeffs, paulis = circuits.pauli_sum(n, 12, seed=5)
+    circ, params = circuits.record(dfs, n, gates)
+    a0 = gaussian_state(rng, 1 << n, normalise=True)
+    psi = dfs.StateVector(n, precision=prec)
+    out = {}
+    for fusion in (True, False):
+        circ.fusion = fusion
+        psi.setAmps(a0)
+        circ.apply(psi, params)
+        out[fusion] = psi.getAllVecAmps()
+    assert rel_err(out[True], out[False]) <= (TOL[prec] if prec != "c64" else 1e-6)
+    if prec != "c64":
+        ref = np.array(a0, dtype=np.complex128)
+        circuits.apply_to(oracle, ref, gates)
+        assert rel_err(out[True], ref) <= TOL[prec]
+    grads = {}
+    for fusion in (True, False):
+        circ.fusion = fusion
+        psi.setAmps(a0)
+        loss = circ.expectation(psi, params, coeffs, paulis)
+        grads[fusion] = (loss, circ.gradient(params))
+    assert abs(grads[True][0] - grads[False][0]) <= (1e-12 if prec != "c64" else 1e-5) * np.sum(np.abs(coeffs))
+    scale = max(1.0, np.max(np.abs(grads[False][1])))
+    assert np.max(np.abs(grads[True][1] - grads[False][1])) <= tol * scale
