@@ -1,11 +1,12 @@
 """The 64-bit index instantiations of every kernel, which states over 2^31 amplitudes
 take (src/types.hpp's Index is 64-bit), checked against the oracle on small states:
 dfs_set_wide_index(1) makes every state take them, and the statevector, density-matrix,
-reduction, adjoint-gradient and allocation-free parity tests run again under it."""
+reduction, adjoint-gradient, paired-gadget and allocation-free parity tests run again under it."""
 import pytest
 
 import test_adjoint_gpu as adj
 import test_dm_gpu as dm
+import test_fusion_gpu as fusion
 import test_sv_gpu as sv
 import test_zz_no_alloc as noalloc
 
@@ -57,6 +58,11 @@ def test_wide_index_reductions(dfs, oracle, rng, wide):
                          ids=lambda f: f.__name__[5:])
 def test_wide_index_adjoint(dfs, oracle, prec, rng, wide, case):
     case(dfs, oracle, prec, rng)
+
+
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-10), ("c64", 2e-4)])
+def test_wide_index_paired_gadgets(dfs, oracle, prec, tol, rng, wide):
+    fusion.test_paired_gadgets(dfs, oracle, prec, tol, rng)
 
 
 @pytest.mark.parametrize("prec", PRECISIONS)
