@@ -337,10 +337,14 @@ static std::vector<AdjTerm> make_terms(unsigned n, const double* coeffs, unsigne
 // 1.08x for the random gate mix's runs of ~5); in complex128 the double-float arithmetic
 // of an operation in shared memory (~2.7 ms) is half a separate HBM-bound kernel
 // (5.3 ms): 1.72x for runs of 30, 1.02x for the gate mix's runs of >= 4 (runs of 3 lost,
-// 0.96x), and the 24-qubit gadget ansatz's forward and backward sweeps 13% and 6% faster.
+// 0.96x).  A run's length is counted in the sweeps its operations take unfused, where
+// consecutive Pauli gadgets go two to a sweep (k_two_gadgets, k_adj_two_gadgets): the
+// 24-qubit gadget ansatz's runs of ~4 gadgets are two such sweeps and run faster that way
+// (complex64 forward 19.0 -> 14.9 ms, backward 37.8 -> 28.0 ms with the backward's
+// threshold raised from 2 to 3 sweeps; complex128 38.4 -> 34.5 and 73.5 -> 65.9 ms).
 static size_t min_run(int precision, bool backward) {
     switch (precision) {
-        case DFS_C64: return backward ? 2 : 3;  // a backward step moves twice the bytes
+        case DFS_C64: return 3;
         case DFS_C128: return 4;
         default: return SIZE_MAX;  // native FP64 arithmetic is bound by the FP64 pipe either way
     }
@@ -405,6 +409,29 @@ static bool param_gadget(const CircOp& op) {
     return (op.kind == OP_PAULI_GADGET || op.kind == OP_PHASE_GADGET) && op.param >= 0;
 }
 
+// two consecutive Pauli gadgets that one sweep applies (k_two_gadgets) or undoes
+// (k_adj_two_gadgets): X parts nonzero and different; the backward pass pairs
+// parametrised gadgets only
+static bool pairable(const CircOp& a, const CircOp& b, bool backward) {
+    if (a.kind != OP_PAULI_GADGET || b.kind != OP_PAULI_GADGET) return false;
+    if (backward && (a.param < 0 || b.param < 0)) return false;
+    uint64_t xa, xb, yz;
+    int ny;
+    pauli_masks(a.targs, a.paulis, 0, &xa, &yz, &ny);
+    pauli_masks(b.targs, b.paulis, 0, &xb, &yz, &ny);
+    return xa != 0 && xb != 0 && xa != xb;
+}
+
+// the sweeps that operations [i, j) take unfused, pairable gadgets two to a sweep
+static size_t separate_sweeps(const Circuit* c, size_t i, size_t j, bool backward) {
+    size_t sweeps = 0;
+    while (i < j) {
+        i += (i + 1 < j && pairable(c->ops[i], c->ops[i + 1], backward)) ? 2 : 1;
+        sweeps++;
+    }
+    return sweeps;
+}
+
 // the runs of a plan with m tile qubits; for the backward sweep (two tiles per CTA, so
 // m is one less) each run's parametrised gadgets get gradRow = their order in the sweep
 // (last operation first), and a run holds at most kFuseMaxParams of them
@@ -437,7 +464,9 @@ static int build_plan(const Circuit* c, int precision, unsigned m, bool backward
             Q = q2;
             j++;
         }
-        if (j - i < std::max<size_t>(2, min_run(precision, backward))) {
+        // a run is fused when it saves enough sweeps: counted as the operations would run
+        // unfused, so a run of gadgets that pair needs twice the length
+        if (separate_sweeps(c, i, j, backward) < std::max<size_t>(2, min_run(precision, backward))) {
             const size_t end = std::max(j, i + 1);
             for (size_t o = i; o < end; o++) pl->segs.push_back({o, o + 1, false, 0, {}, 0});
             i = end;
@@ -556,8 +585,9 @@ static int forward(Circuit* c, State* s, const double* params, bool keepCheckpoi
                 const CircOp& op = c->ops[seg.first];
                 // two consecutive Pauli gadgets with different X parts: one sweep (k_sv.cu)
                 GadgetSpec g1, g2;
-                if (i + 1 < pl->segs.size() && !pl->segs[i + 1].fused && gadget_spec(op, params, &g1) &&
-                    gadget_spec(c->ops[pl->segs[i + 1].first], params, &g2) && g1.x != g2.x) {
+                if (i + 1 < pl->segs.size() && !pl->segs[i + 1].fused &&
+                    pairable(op, c->ops[pl->segs[i + 1].first], false) && gadget_spec(op, params, &g1) &&
+                    gadget_spec(c->ops[pl->segs[i + 1].first], params, &g2)) {
                     rc = sv_two_gadgets(s, g1, g2);
                     i++;
                 } else {
@@ -681,9 +711,8 @@ static int backward(Circuit* c, const double* params, double* grad) {
                 // in one sweep over both vectors, each with its own row of sums
                 const CircOp& op2 = c->ops[seg.first];
                 GadgetSpec g1, g2;
-                if (g > 0 && !pl->segs[g - 1].fused && op2.param >= 0 && c->ops[pl->segs[g - 1].first].param >= 0 &&
-                    gadget_spec(op2, params, &g2) && gadget_spec(c->ops[pl->segs[g - 1].first], params, &g1) &&
-                    g1.x != g2.x) {
+                if (g > 0 && !pl->segs[g - 1].fused && pairable(c->ops[pl->segs[g - 1].first], op2, true) &&
+                    gadget_spec(op2, params, &g2) && gadget_spec(c->ops[pl->segs[g - 1].first], params, &g1)) {
                     const CircOp& op1 = c->ops[pl->segs[g - 1].first];
                     double2* row2 = L.parts + (size_t)uses.size() * L.cols;
                     uses.push_back({op2.param, 0, g2.numY, 2.0});
