@@ -342,7 +342,7 @@ static std::vector<AdjTerm> make_terms(unsigned n, const double* coeffs, unsigne
 // 24-qubit gadget ansatz's runs of ~4 gadgets are two such sweeps and run faster that way
 // (complex64 forward 19.0 -> 14.9 ms, backward 37.8 -> 28.0 ms with the backward's
 // threshold raised from 2 to 3 sweeps; complex128 38.4 -> 34.5 and 73.5 -> 65.9 ms).
-static size_t min_run(int precision, bool backward) {
+static size_t min_run(int precision) {
     switch (precision) {
         case DFS_C64: return 3;
         case DFS_C128: return 4;
@@ -466,7 +466,7 @@ static int build_plan(const Circuit* c, int precision, unsigned m, bool backward
         }
         // a run is fused when it saves enough sweeps: counted as the operations would run
         // unfused, so a run of gadgets that pair needs twice the length
-        if (separate_sweeps(c, i, j, backward) < std::max<size_t>(2, min_run(precision, backward))) {
+        if (separate_sweeps(c, i, j, backward) < std::max<size_t>(2, min_run(precision))) {
             const size_t end = std::max(j, i + 1);
             for (size_t o = i; o < end; o++) pl->segs.push_back({o, o + 1, false, 0, {}, 0});
             i = end;
