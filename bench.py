@@ -42,6 +42,8 @@ CIRCUIT_SEED = 20240611
 STATE_SEED = 77
 # differentiation form: 24-qubit ansatz of 20 layers x 24 Pauli gadgets, H of 100 terms
 ADJ_QUBITS, ADJ_LAYERS, ADJ_PER_LAYER, ADJ_TERMS = 24, 20, 24, 100
+# and its density-matrix variant: 11 qubits, the same layers with channels, H of 40 terms
+ADJ_DM_QUBITS, ADJ_DM_TERMS = 11, 40
 # batched form: 512 circuits of 10..22 qubits, 50 gates each, H of 32 terms
 BATCH_CIRCUITS, BATCH_MIN_Q, BATCH_MAX_Q, BATCH_GATES, BATCH_TERMS, BATCH_SEED = 512, 10, 22, 50, 32, 2024
 # precision form: 32 qubits, the gate mix plus dense k = 2, 4, 5, 6 gates, H of 100 terms
@@ -577,6 +579,30 @@ def adjoint_leg(dfs, circuits, small=False):
         work.free()
     scale = float(np.max(np.abs(grads["c128"])))
     out["c64_gradient_max_rel_err"] = float(np.max(np.abs(grads["c64"] - grads["c128"]))) / scale
+    # the density-matrix variant: 11 qubits, the gadgets' angles and the depolarising and
+    # damping probabilities as parameters (checkpoints before the channels)
+    nd = ADJ_DM_QUBITS
+    dgates = circuits.dm_gadget_ansatz(nd, ADJ_LAYERS, ADJ_PER_LAYER, seed=CIRCUIT_SEED)
+    dcoeffs, dpaulis = circuits.pauli_sum(nd, ADJ_DM_TERMS, seed=12)
+    dcirc, dparams = circuits.record(dfs, nd, dgates, density_matrix=True)
+    rng = np.random.default_rng(4)
+    g = rng.normal(size=(1 << nd, 1 << nd)) + 1j * rng.normal(size=(1 << nd, 1 << nd))
+    rho = g @ g.conj().T
+    rho /= np.trace(rho).real
+    init = dfs.DensityMatrix(nd)
+    init.setMatrix(rho)
+    dcirc.expectation(init, dparams, dcoeffs, dpaulis)
+    dcirc.gradient(dparams)
+    fw, bw = [], []
+    for _ in range(3):
+        fw.append(_sync_time(dfs, lambda: dcirc.expectation(init, dparams, dcoeffs, dpaulis))[0])
+        bw.append(_sync_time(dfs, lambda: dcirc.gradient(dparams))[0])
+    f, b = statistics.median(fw), statistics.median(bw)
+    out["dm_c128"] = {"workload": f"dm{nd} ansatz {ADJ_LAYERS} x ({ADJ_PER_LAYER} Pauli gadgets + depolarising + "
+                                  f"damping), {dparams.size} parameters, H of {ADJ_DM_TERMS} terms",
+                      "forward_ms": f, "backward_ms": b, "gradient_over_forward": (f + b) / f}
+    init.free()
+    dcirc.free()
     return out
 
 

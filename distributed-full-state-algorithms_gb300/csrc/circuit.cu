@@ -658,6 +658,17 @@ static int backward(Circuit* c, const double* params, double* grad) {
                 double a = op.kind == OP_PAULI_GADGET && odd_y(ps) ? 1.0 : -1.0;
                 pauli_masks(op.targs, ps, n, &mX, &mYZ, &numY);
                 double2* row = L.parts + (size_t)uses.size() * L.cols;
+                if (mX != 0) {
+                    // ket and bra halves (X and X << n) undone in one sweep, a row for each
+                    uint64_t kX, kYZ;
+                    int kY;
+                    pauli_masks(op.targs, ps, 0, &kX, &kYZ, &kY);
+                    uses.push_back({op.param, 0, numY, a});
+                    double2* rowKet = L.parts + (size_t)uses.size() * L.cols;
+                    uses.push_back({op.param, 0, kY, 1.0});
+                    return adj_two_gadgets_step(st, ad, GadgetSpec{kX, kYZ, kY, v}, GadgetSpec{mX, mYZ, numY, a * v},
+                                                rowKet, row);
+                }
                 if ((rc = adj_gadget_step(st, ad, mX, mYZ, numY, a * v, row))) return rc;
                 uses.push_back({op.param, 0, numY, a});
             }
