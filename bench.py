@@ -433,8 +433,9 @@ def gpu_arm(args, world, rank, local):
         lib = dfs.load_library()
         hosts = [torch.empty(num_amps * 2, dtype=torch.float64, pin_memory=True)]
         psi2 = None
-        try:  # the serving loop's second pinned buffer and device state
-            hosts.append(torch.empty(num_amps * 2, dtype=torch.float64, pin_memory=True))
+        try:  # the serving loop's pinned input and output buffers (two each) and second state
+            for _ in range(3):
+                hosts.append(torch.empty(num_amps * 2, dtype=torch.float64, pin_memory=True))
             psi2 = dfs.StateVector(n)
         except (RuntimeError, dfs.DfsError):
             pass
@@ -466,27 +467,28 @@ def gpu_arm(args, world, rank, local):
                     "median_s": {"upload": med[0], "circuit": med[1], "download": med[2]},
                     "host_link_gbs": {"h2d": num_amps * elem / med[0] / 1e9, "d2h": num_amps * elem / med[2] / 1e9}}
         if serving:
-            # the same as a serving loop: the transfers go on the engine's copy stream
-            # (dfs_state_set_raw_async / get_raw_async), so step i+1's upload and step i-1's
-            # download overlap step i's gates; two device states, two pinned buffers (step
-            # i + 2 takes step i's output as its input)
+            # the same as a serving loop: the transfers go on the engine's copy streams
+            # (dfs_state_set_raw_async / get_raw_async, one stream per direction), so step
+            # i+1's upload and step i-1's download overlap step i's gates and each other; two
+            # device states, two pinned input buffers and two pinned output buffers
+            ins, outs = hosts[:2], hosts[2:]
             states = [psi, psi2]
             barrier()
             t0 = time.perf_counter()
-            states[0].uploadAsync(hosts[0])
+            states[0].uploadAsync(ins[0])
             for i in range(e2e_steps):
                 cur, nxt = states[i % 2], states[(i + 1) % 2]
                 if i + 1 < e2e_steps:
-                    nxt.uploadAsync(hosts[(i + 1) % 2])
+                    nxt.uploadAsync(ins[(i + 1) % 2])
                 circuits.apply(dfs, cur, gates)
-                cur.downloadAsync(hosts[i % 2])
+                cur.downloadAsync(outs[i % 2])
             for st in states:
                 st.waitTransfers()
             dfs.comm_synch()
             barrier()
             e2e_s = time.perf_counter() - t0
             result["e2e"] = {"value": world * len(gates) * e2e_steps / e2e_s, "unit": "gates/s", **per_step,
-                             "mode": f"serving loop of {e2e_steps} steps, transfers overlapped on a copy stream"}
+                             "mode": f"serving loop of {e2e_steps} steps, transfers overlapped on two copy streams"}
             result["e2e_blocking"] = blocking
         else:  # no room for a second state or pinned buffer on some rank
             result["e2e"] = blocking

@@ -406,33 +406,36 @@ int dfs_state_get_raw(dfs_state s, void* dst, uint64_t start, uint64_t count) {
     return e == cudaSuccess ? DFS_SUCCESS : cuda_fail(e, "get_raw");
 }
 
-// asynchronous raw transfer on the copy stream, after the work already queued on the
-// compute stream (which covers every earlier operation on the state) and, in stream
-// order, after the state's earlier transfers
+// asynchronous raw transfer on a copy stream (one per direction), after the work already
+// queued on the compute stream (which covers every earlier operation on the state) and
+// after the state's earlier transfer when it is still pending (on either stream)
 static int transfer_async(dfs_state s, void* host, uint64_t start, uint64_t count, bool toDevice) {
-    // no state_acquire: the copy stream orders this after the state's earlier transfers,
-    // and the compute stream must not wait for them here
+    // no state_acquire: the compute stream must not wait for the state's transfers here
     int rc = check_range(s, host, start, count, false);
     if (rc || !count) return rc;
     cudaError_t e = cudaSuccess;
     if (!g_ctx.copyStream) e = cudaStreamCreateWithFlags(&g_ctx.copyStream, cudaStreamNonBlocking);
+    if (e == cudaSuccess && !g_ctx.copyStreamD2H) e = cudaStreamCreateWithFlags(&g_ctx.copyStreamD2H, cudaStreamNonBlocking);
     if (e == cudaSuccess && !g_ctx.computeMark) e = cudaEventCreateWithFlags(&g_ctx.computeMark, cudaEventDisableTiming);
     if (e == cudaSuccess && !s->copyDone) e = cudaEventCreateWithFlags(&s->copyDone, cudaEventDisableTiming);
+    cudaStream_t cs = toDevice ? g_ctx.copyStream : g_ctx.copyStreamD2H;
     if (e == cudaSuccess) e = cudaEventRecord(g_ctx.computeMark, g_ctx.stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(g_ctx.copyStream, g_ctx.computeMark, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, g_ctx.computeMark, 0);
+    // the state's previous transfer (an upload before this download, or the reverse) first
+    if (e == cudaSuccess && s->copyPending) e = cudaStreamWaitEvent(cs, s->copyDone, 0);
     const size_t eb = elem_bytes(s->precision);
     char* dev = (char*)s->amps + start * eb;
     if (e == cudaSuccess)
-        e = toDevice ? cudaMemcpyAsync(dev, host, count * eb, cudaMemcpyHostToDevice, g_ctx.copyStream)
-                     : cudaMemcpyAsync(host, dev, count * eb, cudaMemcpyDeviceToHost, g_ctx.copyStream);
+        e = toDevice ? cudaMemcpyAsync(dev, host, count * eb, cudaMemcpyHostToDevice, cs)
+                     : cudaMemcpyAsync(host, dev, count * eb, cudaMemcpyDeviceToHost, cs);
     if (e != cudaSuccess) return cuda_fail(e, "asynchronous state transfer");
     // new content: its magnitudes are measured right behind the copy, on the copy stream,
     // and read back by the first operation that needs them
     if (toDevice) {
-        int rc2 = range_measure_async(s, g_ctx.copyStream);
+        int rc2 = range_measure_async(s, cs);
         if (rc2) return rc2;
     }
-    e = cudaEventRecord(s->copyDone, g_ctx.copyStream);
+    e = cudaEventRecord(s->copyDone, cs);
     if (e != cudaSuccess) return cuda_fail(e, "asynchronous state transfer");
     s->copyPending = true;
     return DFS_SUCCESS;

@@ -32,8 +32,10 @@ struct Context {
     // 64-bit index maths for every state, not only those over 2^31 amplitudes
     // (dfs_set_wide_index: those kernel instantiations checked at small sizes)
     bool wideIndex = false;
-    // asynchronous host transfers (dfs_state_*_raw_async) run here, beside `stream`
-    cudaStream_t copyStream = nullptr;
+    // asynchronous host transfers (dfs_state_*_raw_async) run here, beside `stream`: uploads
+    // and downloads on streams of their own, so that the two directions overlap
+    cudaStream_t copyStream = nullptr;   // host -> device
+    cudaStream_t copyStreamD2H = nullptr;  // device -> host
     cudaEvent_t computeMark = nullptr;
 };
 
