@@ -78,10 +78,6 @@ __global__ void __launch_bounds__(kThreads) k_adj_gadget_pair(typename P::store*
     if (threadIdx.x == 0) partials[blockIdx.x] = sum_to_double2(s);
 }
 
-// Two consecutive gadgets G2 G1 (X1 != X2, both nonzero) undone in one sweep over both
-// vectors, on the quads {r, r^X1, r^X2, r^X1^X2} of the forward kernel (k_sv.cu
-// k_two_gadgets): g2's sums from the vectors after G2, then both <- G2^dag in registers,
-// g1's sums, both <- G1^dag, one store.  Half the bytes of two k_adj_gadget_pair sweeps.
 // per-thread sums of conj(a) b: Dot2 accumulators in double-float, else the policy's sum
 template <class P>
 struct ConjAcc {
@@ -102,6 +98,10 @@ struct ConjAcc<PolDF> {
     DEV SumDF total() const { return SumDF{df::acc_result(re), df::acc_result(im)}; }
 };
 
+// Two consecutive gadgets G2 G1 (X1 != X2, both nonzero) undone in one sweep over both
+// vectors, on the quads {r, r^X1, r^X2, r^X1^X2} of the forward kernel (k_sv.cu
+// k_two_gadgets): g2's sums from the vectors after G2, then both <- G2^dag in registers,
+// g1's sums, both <- G1^dag, one store.  Half the bytes of two k_adj_gadget_pair sweeps.
 template <class P, class IT>
 struct AdjTwoGadgetOp {
     typename P::R c1, sn1, c2, sn2;  // cos and -sin of each angle (the inverse gadgets)
