@@ -111,11 +111,13 @@ struct AdjTwoGadgetOp {
 
 // three CTAs per SM (80 registers, a few spilled): the 11-qubit density-matrix ansatz's
 // backward 40.1 -> 38.0 ms with the Dot2 sums, the 24-qubit complex128 one 3% faster
-template <class P, class IT>
+// kOdd1, kOdd2: the parities of m1, m2 (fixed re/im swaps, as in k_two_gadgets)
+template <class P, class IT, int kOdd1, int kOdd2>
 __global__ void __launch_bounds__(kThreads, 3) k_adj_two_gadgets(typename P::store* __restrict__ st,
                                                               typename P::store* __restrict__ ad, IT items,
                                                               AdjTwoGadgetOp<P, IT> op, double2* __restrict__ parts1,
                                                               double2* __restrict__ parts2) {
+    const int h1 = (op.m1 >> 1) & 1, h2 = (op.m2 >> 1) & 1;
     ConjAcc<P> A1, A2;
     A1.zero();
     A2.zero();
@@ -141,15 +143,15 @@ __global__ void __launch_bounds__(kThreads, 3) k_adj_two_gadgets(typename P::sto
 #pragma unroll
         for (int e = 0; e < 2; e++) {
             typename P::A a0 = P::first_r(op.c2, x[e]);
-            P::mac_r(a0, op.sn2, rot<P>(x[e ^ 2], op.m2, sg2[e]));
+            P::mac_r(a0, op.sn2, rot<P>(x[e ^ 2], kOdd2, sg2[e] ^ h2));
             typename P::A a1 = P::first_r(op.c2, x[e ^ 2]);
-            P::mac_r(a1, op.sn2, rot<P>(x[e], op.m2, sg2[e ^ 2]));
+            P::mac_r(a1, op.sn2, rot<P>(x[e], kOdd2, sg2[e ^ 2] ^ h2));
             x[e] = P::get(a0);
             x[e ^ 2] = P::get(a1);
             typename P::A b0 = P::first_r(op.c2, l[e]);
-            P::mac_r(b0, op.sn2, rot<P>(l[e ^ 2], op.m2, sg2[e]));
+            P::mac_r(b0, op.sn2, rot<P>(l[e ^ 2], kOdd2, sg2[e] ^ h2));
             typename P::A b1 = P::first_r(op.c2, l[e ^ 2]);
-            P::mac_r(b1, op.sn2, rot<P>(l[e], op.m2, sg2[e ^ 2]));
+            P::mac_r(b1, op.sn2, rot<P>(l[e], kOdd2, sg2[e ^ 2] ^ h2));
             l[e] = P::get(b0);
             l[e ^ 2] = P::get(b1);
         }
@@ -159,15 +161,15 @@ __global__ void __launch_bounds__(kThreads, 3) k_adj_two_gadgets(typename P::sto
 #pragma unroll
         for (int e = 0; e < 4; e += 2) {
             typename P::A a0 = P::first_r(op.c1, x[e]);
-            P::mac_r(a0, op.sn1, rot<P>(x[e ^ 1], op.m1, sg1[e]));
+            P::mac_r(a0, op.sn1, rot<P>(x[e ^ 1], kOdd1, sg1[e] ^ h1));
             typename P::A a1 = P::first_r(op.c1, x[e ^ 1]);
-            P::mac_r(a1, op.sn1, rot<P>(x[e], op.m1, sg1[e ^ 1]));
+            P::mac_r(a1, op.sn1, rot<P>(x[e], kOdd1, sg1[e ^ 1] ^ h1));
             P::save(st, idx[e], P::get(a0));
             P::save(st, idx[e ^ 1], P::get(a1));
             typename P::A b0 = P::first_r(op.c1, l[e]);
-            P::mac_r(b0, op.sn1, rot<P>(l[e ^ 1], op.m1, sg1[e]));
+            P::mac_r(b0, op.sn1, rot<P>(l[e ^ 1], kOdd1, sg1[e] ^ h1));
             typename P::A b1 = P::first_r(op.c1, l[e ^ 1]);
-            P::mac_r(b1, op.sn1, rot<P>(l[e], op.m1, sg1[e ^ 1]));
+            P::mac_r(b1, op.sn1, rot<P>(l[e], kOdd1, sg1[e ^ 1] ^ h1));
             P::save(ad, idx[e], P::get(b0));
             P::save(ad, idx[e ^ 1], P::get(b1));
         }
@@ -418,8 +420,14 @@ struct RunAdjTwoGadgets {
         op.m1 = (g1.numY + 1) & 3;
         op.m2 = (g2.numY + 1) & 3;
         IT items = (IT)(st->numAmps / 4);
-        k_adj_two_gadgets<P, IT><<<adj_grid(items), kThreads, 0, ctx().stream>>>((S*)st->amps, (S*)ad->amps, items, op,
-                                                                                 row1, row2);
+        auto kern = k_adj_two_gadgets<P, IT, 1, 1>;
+        switch ((op.m1 & 1) * 2 + (op.m2 & 1)) {
+            case 0: kern = k_adj_two_gadgets<P, IT, 0, 0>; break;
+            case 1: kern = k_adj_two_gadgets<P, IT, 0, 1>; break;
+            case 2: kern = k_adj_two_gadgets<P, IT, 1, 0>; break;
+            default: break;
+        }
+        kern<<<adj_grid(items), kThreads, 0, ctx().stream>>>((S*)st->amps, (S*)ad->amps, items, op, row1, row2);
         return check_launch("adjoint of two gadgets");
     }
 };

@@ -197,9 +197,12 @@ struct TwoGadgetOp {
     int m1, m2;  // #Y + 1 of each string: the power of i of its gadget term
 };
 
-template <class P, class IT>
+// kOdd1, kOdd2: the parities of m1, m2 as template parameters, so that each term's re/im
+// swap is fixed and only its sign (i^2 = -1 folded in) is chosen at run time
+template <class P, class IT, int kOdd1, int kOdd2>
 __global__ void __launch_bounds__(kThreads) k_two_gadgets(typename P::store* __restrict__ a, IT items,
                                                           TwoGadgetOp<P, IT> op) {
+    const int h1 = (op.m1 >> 1) & 1, h2 = (op.m2 >> 1) & 1, h12 = ((op.m1 + op.m2) >> 1) & 1;
     const IT stride = (IT)gridDim.x * kThreads;
     for (IT j = (IT)blockIdx.x * kThreads + threadIdx.x; j < items; j += stride) {
         const IT r = insert_zero(insert_zero(j, op.lo), op.hi);
@@ -212,9 +215,9 @@ __global__ void __launch_bounds__(kThreads) k_two_gadgets(typename P::store* __r
             const int s1 = parity(idx[e ^ 1] & op.yz1), s2 = parity(idx[e ^ 2] & op.yz2);
             const int s21 = s2 ^ parity(idx[e ^ 3] & op.yz1);
             typename P::A acc = P::first_r(op.c12, x[e]);
-            P::mac_r(acc, op.cs1, rot<P>(x[e ^ 1], op.m1, s1));
-            P::mac_r(acc, op.cs2, rot<P>(x[e ^ 2], op.m2, s2));
-            P::mac_r(acc, op.ss, rot<P>(x[e ^ 3], op.m1 + op.m2, s21));
+            P::mac_r(acc, op.cs1, rot<P>(x[e ^ 1], kOdd1, s1 ^ h1));
+            P::mac_r(acc, op.cs2, rot<P>(x[e ^ 2], kOdd2, s2 ^ h2));
+            P::mac_r(acc, op.ss, rot<P>(x[e ^ 3], kOdd1 ^ kOdd2, s21 ^ h12));
             P::save(a, idx[e], P::get(acc));
         }
     }
@@ -238,7 +241,13 @@ struct RunTwoGadgets {
         op.m1 = (g1.numY + 1) & 3;
         op.m2 = (g2.numY + 1) & 3;
         IT items = (IT)(s->numAmps / 4);
-        return launch(k_two_gadgets<P, IT>, items, 1, "two Pauli gadgets", (typename P::store*)s->amps, items, op);
+        typename P::store* amps = (typename P::store*)s->amps;
+        switch ((op.m1 & 1) * 2 + (op.m2 & 1)) {
+            case 0: return launch(k_two_gadgets<P, IT, 0, 0>, items, 1, "two Pauli gadgets", amps, items, op);
+            case 1: return launch(k_two_gadgets<P, IT, 0, 1>, items, 1, "two Pauli gadgets", amps, items, op);
+            case 2: return launch(k_two_gadgets<P, IT, 1, 0>, items, 1, "two Pauli gadgets", amps, items, op);
+            default: return launch(k_two_gadgets<P, IT, 1, 1>, items, 1, "two Pauli gadgets", amps, items, op);
+        }
     }
 };
 int sv_two_gadgets(State* s, const GadgetSpec& g1, const GadgetSpec& g2) {
