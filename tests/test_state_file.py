@@ -137,6 +137,40 @@ def test_async_transfers_order_with_gates(dfs, oracle, rng, prec):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+def test_async_transfers_back_to_back(dfs, rng, prec):
+    """Uploads and downloads of one state with no operation between them (they run on the
+    two copy streams, one per direction) land in the order they were issued, whole and
+    partial."""
+    n = 18
+    N, half = 1 << n, 1 << (n - 1)
+    dt = np.complex64 if prec == "c64" else np.complex128
+    a = gaussian_state(rng, N).astype(dt)
+    c = gaussian_state(rng, N).astype(dt)
+    h = gaussian_state(rng, half).astype(dt)
+    ta, ha = _pinned(N, dt)
+    tb, hb = _pinned(N, dt)
+    tc, hc = _pinned(N, dt)
+    td, hd = _pinned(N, dt)
+    th, hh = _pinned(half, dt)
+    te, he = _pinned(N, dt)
+    ha[:], hc[:], hh[:] = a, c, h
+    psi = dfs.StateVector(n, precision=prec)
+    psi.uploadAsync(ta)
+    psi.downloadAsync(tb)
+    psi.uploadAsync(tc)
+    psi.downloadAsync(td)
+    psi.uploadAsync(th, start=half)  # the upper half replaced
+    psi.downloadAsync(te)
+    psi.waitTransfers()
+    assert np.array_equal(hb, a)
+    assert np.array_equal(hd, c)
+    want = c.copy()
+    want[half:] = h
+    assert np.array_equal(he, want)
+
+
+@pytest.mark.gpu
 def test_async_pipeline_two_states(dfs, oracle, rng):
     """The serving loop of the end-to-end benchmark: state i+1 uploads and state i-1
     downloads while state i runs its gates."""
