@@ -33,6 +33,16 @@ DEV IT ins(IT j, const OpD& op) {
     }
     return j;
 }
+// the same for a record whose qubit count NQ is known at compile time: unrolled
+template <int NQ>
+DEV IT ins_n(IT j, const OpD& op) {
+#pragma unroll
+    for (int s = 0; s < NQ; s++) {
+        const IT low = ((IT)1 << op.q[s]) - 1;
+        j = ((j & ~low) << 1) | (j & low);
+    }
+    return j;
+}
 
 // The items of a span, U at a time while a thread has U of them left: the U items'
 // loads are all issued before the first result is stored, which the compiler cannot do
@@ -66,8 +76,10 @@ DEV void stage_gate(const double* m, int count, typename P::K* sG) {
 
 // ------------------------------------------------------------- operations
 
-template <class P, int U = span_unroll<P>()>
-DEV void op_pair(const OpD& op, typename P::store* x, IT N, Span sp, const typename P::K* g) {
+// NQ: the record's qubit count when it is known here (1 for a gate without
+// controls), else 0 (the loop over the record's qubits)
+template <class P, int U, int NQ>
+DEV void op_pair_n(const OpD& op, typename P::store* x, IT N, Span sp, const typename P::K* g) {
     const typename P::K g0 = g[0], g1 = g[1], g2 = g[2], g3 = g[3];
     struct Rec {
         IT i0, i1;
@@ -77,7 +89,8 @@ DEV void op_pair(const OpD& op, typename P::store* x, IT N, Span sp, const typen
         N >> op.nq, sp,
         [&](IT j) {
             Rec r;
-            r.i1 = ins(j, op) | op.setMask;
+            if constexpr (NQ > 0) r.i1 = ins_n<NQ>(j, op) | op.setMask;
+            else r.i1 = ins(j, op) | op.setMask;
             r.i0 = r.i1 ^ op.tbit;
             r.x0 = P::load(x, r.i0);
             r.x1 = P::load(x, r.i1);
@@ -93,6 +106,12 @@ DEV void op_pair(const OpD& op, typename P::store* x, IT N, Span sp, const typen
         });
 }
 
+template <class P, int U = span_unroll<P>()>
+DEV void op_pair(const OpD& op, typename P::store* x, IT N, Span sp, const typename P::K* g) {
+    if (op.nq == 1) op_pair_n<P, U, 1>(op, x, N, sp, g);
+    else op_pair_n<P, U, 0>(op, x, N, sp, g);
+}
+
 template <class S, int U = sizeof(S) == 16 ? 2 : 4>
 DEV void op_swap(const OpD& op, S* x, IT N, Span sp) {
     struct Rec {
@@ -103,7 +122,7 @@ DEV void op_swap(const OpD& op, S* x, IT N, Span sp) {
         N >> 2, sp,
         [&](IT j) {
             Rec r;
-            const IT b = ins(j, op);
+            const IT b = ins_n<2>(j, op);  // a swap's record holds its two qubits
             r.i0 = b | op.setMask;
             r.i1 = b | op.tbit;
             r.a = x[r.i0];
@@ -124,7 +143,7 @@ DEV void op_dense(const OpD& op, typename P::store* x, IT N, Span sp, const type
     for (int c = 0; c < D; c++) off[c] = op.off[c];
     const IT items = N >> K;
     for (IT j = sp.first; j < items; j += sp.stride) {
-        IT b = ins(j, op);
+        IT b = ins_n<K>(j, op);  // a dense record holds its K targets
         typename P::V v[D];
 #pragma unroll
         for (int c = 0; c < D; c++) v[c] = P::load(x, b + off[c]);
