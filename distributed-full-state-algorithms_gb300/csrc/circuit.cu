@@ -333,11 +333,11 @@ static std::vector<AdjTerm> make_terms(unsigned n, const double* coeffs, unsigne
 // each run of at least min_run operations is one pass of k_fused_run, every other
 // operation runs as its own kernel.  The plan depends only on the operations and the
 // precision.  Measured at 30 qubits: in complex64 a run costs about one HBM pass plus
-// ~1 ms of shared-memory work per operation (2.5x over separate kernels for runs of 40,
-// 1.08x for the random gate mix's runs of ~5); in complex128 the double-float arithmetic
-// of an operation in shared memory (~2.7 ms) is half a separate HBM-bound kernel
-// (5.3 ms): 1.72x for runs of 30, 1.02x for the gate mix's runs of >= 4 (runs of 3 lost,
-// 0.96x).  A run's length is counted in the sweeps its operations take unfused, where
+// ~1 ms of shared-memory work per operation (3.0x over separate kernels for runs of 40,
+// 1.14x for the random gate mix's runs of ~5); in complex128 the double-float arithmetic
+// of an operation in shared memory (~2.8 ms) is half a separate HBM-bound kernel
+// (5.3 ms): 1.63x for a circuit of low-qubit gates, 1.04x for the gate mix's runs of >= 4
+// (with runs of 3 fused too, 0.98x).  A run's length is counted in the sweeps its operations take unfused, where
 // consecutive Pauli gadgets go two to a sweep (k_two_gadgets, k_adj_two_gadgets): the
 // 24-qubit gadget ansatz's runs of ~4 gadgets are two such sweeps and run faster that way
 // (complex64 forward 19.0 -> 14.9 ms, backward 37.8 -> 28.0 ms with the backward's

@@ -76,7 +76,7 @@ DEV void stage_gate(const double* m, int count, typename P::K* sG) {
 
 // ------------------------------------------------------------- operations
 
-// NQ: the record's qubit count when it is known here (1 for a gate without
+// NQ: the record's qubit count when it is known here (the target and up to two
 // controls), else 0 (the loop over the record's qubits)
 template <class P, int U, int NQ>
 DEV void op_pair_n(const OpD& op, typename P::store* x, IT N, Span sp, const typename P::K* g) {
@@ -108,8 +108,12 @@ DEV void op_pair_n(const OpD& op, typename P::store* x, IT N, Span sp, const typ
 
 template <class P, int U = span_unroll<P>()>
 DEV void op_pair(const OpD& op, typename P::store* x, IT N, Span sp, const typename P::K* g) {
-    if (op.nq == 1) op_pair_n<P, U, 1>(op, x, N, sp, g);
-    else op_pair_n<P, U, 0>(op, x, N, sp, g);
+    switch (op.nq) {
+        case 1: op_pair_n<P, U, 1>(op, x, N, sp, g); break;
+        case 2: op_pair_n<P, U, 2>(op, x, N, sp, g); break;
+        case 3: op_pair_n<P, U, 3>(op, x, N, sp, g); break;
+        default: op_pair_n<P, U, 0>(op, x, N, sp, g); break;
+    }
 }
 
 template <class S, int U = sizeof(S) == 16 ? 2 : 4>
