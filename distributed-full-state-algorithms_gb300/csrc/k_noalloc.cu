@@ -21,8 +21,7 @@
 //    so no slot has to start at zero, but calls whose kernels overlap on the GPU
 //    (different streams or host threads) race on it and must be serialised;
 //  - the first call on each device looks up the array's device address with
-//    cudaGetSymbolAddress (with the engine's device current); make that first
-//    call before any stream capture;
+//    cudaGetSymbolAddress (with the engine's device current);
 //  - a complex128 matrix whose magnitudes the engine has not measured yet is
 //    summed with native FP64 arithmetic (measuring would allocate).
 #include <algorithm>

@@ -271,7 +271,7 @@ int dfs_densitymatrix_trace(dfs_state s, double* out_re, double* out_im);
  * must be serialised by the caller.  The call is synchronous, like the ordinary one: it reads
  * the result back and synchronises the engine's stream before it returns.  The first call on
  * each device looks the array's address up with cudaGetSymbolAddress (with the engine's
- * device current), so make it before any stream capture begins.  A complex128 matrix whose
+ * device current).  A complex128 matrix whose
  * magnitudes the engine has not yet measured (right after an upload) is summed with native
  * FP64 arithmetic, since measuring would allocate.  Results equal
  * dfs_densitymatrix_expecPauliString's within rounding. */
