@@ -29,19 +29,28 @@ struct ChannelMats {
 };
 
 unsigned adj_partial_cols();
+// The steps below take raw = true when the complex128 vectors they touch hold
+// double-float pairs (PolDFraw) rather than IEEE doubles; adj_convert moves a
+// vector between the two forms.
+//
+// dst <- src converted to double-float pairs (toRaw) or back to IEEE doubles; dst may
+// be src.  Complex128 states in double-float arithmetic only.
+int adj_convert(State* dst, const State* src, bool toRaw);
 // partial sums of sum_j conj(ad_j) (-1)^{par((j^X)&YZ)} st_{j^X} into row[0..cols),
 // then st, ad <- exp(-i phi Q)
-int adj_gadget_step(State* st, State* ad, uint64_t maskX, uint64_t maskYZ, int numY, double phi, double2* row);
+int adj_gadget_step(State* st, State* ad, uint64_t maskX, uint64_t maskYZ, int numY, double phi, double2* row,
+                    bool raw = false);
 // the same for two gadgets in one sweep over both vectors (g2 the later one, undone
 // first): g2's partial sums into row2, g1's into row1, then st, ad <- G1^dag G2^dag
 int adj_two_gadgets_step(State* st, State* ad, const GadgetSpec& g1, const GadgetSpec& g2, double2* row1,
-                         double2* row2);
+                         double2* row2, bool raw = false);
 // out <- H psi; partial sums of <psi|out> into row
 int adj_pauli_sum_apply(State* psi, State* out, const AdjTerm* terms, unsigned numTerms, double2* row);
 // s <- vec(H) of a density matrix
 int adj_dm_pauli_sum_build(State* s, const AdjTerm* terms, unsigned numTerms);
 // partial sums of <ad, D rho> into row (when rho and row are given), then ad <- S^T ad
-int adj_channel_step(State* ad, const State* rho, const ChannelMats<1>* m1, const ChannelMats<2>* m2, double2* row);
+int adj_channel_step(State* ad, const State* rho, const ChannelMats<1>* m1, const ChannelMats<2>* m2, double2* row,
+                     bool raw = false);
 // out[r] = sum of row r of parts (rows x cols), in a fixed order
 int adj_sum_rows(const double2* parts, unsigned rows, unsigned cols, double2* out, cudaStream_t stream = nullptr);
 

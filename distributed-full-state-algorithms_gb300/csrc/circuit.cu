@@ -627,6 +627,37 @@ struct RowUse {
     double weight;
 };
 
+// Complex128 backward sweeps in double-float arithmetic keep both private vectors as
+// double-float pairs (PolDFraw) over stretches of steps whose kernels read that form
+// (gadgets, channels, fused runs), so that those sweeps skip the IEEE decode and
+// encode; the ordinary kernels of any other step read IEEE doubles.  Entering a
+// stretch converts both vectors and leaving it converts them back (one sweep of each
+// either way); the sweep ends without converting back (the next dfs_circuit_expec
+// rewrites both vectors).  A stretch is taken in that form when it is at least
+// kRawStretch steps long, or kRawStretchLast when it ends the sweep.
+constexpr size_t kRawStretch = 8, kRawStretchLast = 4;
+
+static std::vector<char> raw_stretches(const std::vector<char>& capable) {
+    std::vector<char> want(capable.size(), 0);
+    for (size_t a = 0; a < capable.size();) {
+        if (!capable[a]) {
+            a++;
+            continue;
+        }
+        size_t b = a;
+        while (b < capable.size() && capable[b]) b++;
+        if (b - a >= (b == capable.size() ? kRawStretchLast : kRawStretch))
+            std::fill(want.begin() + (long)a, want.begin() + (long)b, 1);
+        a = b;
+    }
+    return want;
+}
+
+// a step whose kernels take double-float pairs: a parametrised gadget or a channel
+static bool raw_capable(const CircOp& op) {
+    return ((op.kind == OP_PAULI_GADGET || op.kind == OP_PHASE_GADGET) && op.param >= 0) || op.is_channel();
+}
+
 static int backward(Circuit* c, const double* params, double* grad) {
     DevLayout L;
     int rc = ensure_dev(c, (unsigned)c->terms.size(), &L);
@@ -644,6 +675,16 @@ static int backward(Circuit* c, const double* params, double* grad) {
     }
     std::vector<RowUse> uses;
     size_t k = c->ckpt.size();
+    const bool rawOk = st->precision == DFS_C128 && !st->forceNative && !ad->forceNative;
+    bool raw = false;  // st and ad hold double-float pairs
+    auto set_raw = [&](bool want) -> int {
+        want = want && rawOk;
+        if (want == raw) return DFS_SUCCESS;
+        int rc = adj_convert(st, st, want);
+        if (!rc) rc = adj_convert(ad, ad, want);
+        if (!rc) raw = want;
+        return rc;
+    };
     auto undo = [&](size_t i) -> int {
         int rc = DFS_SUCCESS;
         const CircOp& op = c->ops[i];
@@ -667,20 +708,25 @@ static int backward(Circuit* c, const double* params, double* grad) {
                     double2* rowKet = L.parts + (size_t)uses.size() * L.cols;
                     uses.push_back({op.param, 0, kY, 1.0});
                     return adj_two_gadgets_step(st, ad, GadgetSpec{kX, kYZ, kY, v}, GadgetSpec{mX, mYZ, numY, a * v},
-                                                rowKet, row);
+                                                rowKet, row, raw);
                 }
-                if ((rc = adj_gadget_step(st, ad, mX, mYZ, numY, a * v, row))) return rc;
+                if ((rc = adj_gadget_step(st, ad, mX, mYZ, numY, a * v, row, raw))) return rc;
                 uses.push_back({op.param, 0, numY, a});
             }
             pauli_masks(op.targs, ps, 0, &mX, &mYZ, &numY);
             double2* row = L.parts + (size_t)uses.size() * L.cols;
-            if ((rc = adj_gadget_step(st, ad, mX, mYZ, numY, v, row))) return rc;
+            if ((rc = adj_gadget_step(st, ad, mX, mYZ, numY, v, row, raw))) return rc;
             uses.push_back({op.param, 0, numY, c->isDM ? 1.0 : 2.0});
             return DFS_SUCCESS;
         }
         if (op.is_channel()) {
             State* before = c->ckpt[--k];
-            if ((rc = dfs_state_copy(static_cast<dfs_state>(st), static_cast<dfs_state>(before)))) return rc;
+            if (raw) {
+                range_copy(st, before);
+                if ((rc = adj_convert(st, before, true))) return rc;
+            } else if ((rc = dfs_state_copy(static_cast<dfs_state>(st), static_cast<dfs_state>(before)))) {
+                return rc;
+            }
             double2* row = nullptr;
             if (op.param >= 0) {
                 row = L.parts + (size_t)uses.size() * L.cols;
@@ -689,11 +735,11 @@ static int backward(Circuit* c, const double* params, double* grad) {
             if (op.kind == OP_DEPH2 || op.kind == OP_DEPOL2) {
                 ChannelMats<2> m;
                 channel_mats2(op, n, v, &m);
-                rc = adj_channel_step(ad, st, nullptr, &m, row);
+                rc = adj_channel_step(ad, st, nullptr, &m, row, raw);
             } else {
                 ChannelMats<1> m;
                 channel_mats1(op, n, v, &m);
-                rc = adj_channel_step(ad, st, &m, nullptr, row);
+                rc = adj_channel_step(ad, st, &m, nullptr, row, raw);
             }
             return rc;
         }
@@ -715,8 +761,14 @@ static int backward(Circuit* c, const double* params, double* grad) {
     }
     if (pl) {
         if ((rc = upload_angles(c, pl, params))) return rc;
-        for (size_t g = pl->segs.size(); g-- > 0;) {
+        const size_t S = pl->segs.size();
+        std::vector<char> capable(S);
+        for (size_t g = 0; g < S; g++)
+            capable[S - 1 - g] = pl->segs[g].fused || raw_capable(c->ops[pl->segs[g].first]);
+        const std::vector<char> want = raw_stretches(capable);
+        for (size_t g = S; g-- > 0;) {
             const FusedSeg& seg = pl->segs[g];
+            if ((rc = set_raw(want[S - 1 - g]))) return rc;
             if (!seg.fused) {
                 // two consecutive parametrised Pauli gadgets with different X parts: undone
                 // in one sweep over both vectors, each with its own row of sums
@@ -729,7 +781,7 @@ static int backward(Circuit* c, const double* params, double* grad) {
                     uses.push_back({op2.param, 0, g2.numY, 2.0});
                     double2* row1 = L.parts + (size_t)uses.size() * L.cols;
                     uses.push_back({op1.param, 0, g1.numY, 2.0});
-                    if ((rc = adj_two_gadgets_step(st, ad, g1, g2, row1, row2))) return rc;
+                    if ((rc = adj_two_gadgets_step(st, ad, g1, g2, row1, row2, raw))) return rc;
                     g--;
                     continue;
                 }
@@ -737,7 +789,7 @@ static int backward(Circuit* c, const double* params, double* grad) {
                 continue;
             }
             const unsigned rowBase = (unsigned)uses.size();
-            if ((rc = fused_run_backward(st, ad, launch_of(pl, seg, n), L.parts, L.cols, rowBase))) return rc;
+            if ((rc = fused_run_backward(st, ad, launch_of(pl, seg, n), L.parts, L.cols, rowBase, raw))) return rc;
             for (size_t o = seg.last; o-- > seg.first;) {
                 const CircOp& op = c->ops[o];
                 if (!param_gadget(op)) continue;
@@ -750,8 +802,14 @@ static int backward(Circuit* c, const double* params, double* grad) {
             }
         }
     } else {
-        for (size_t i = c->ops.size(); i-- > 0;)
+        const size_t S = c->ops.size();
+        std::vector<char> capable(S);
+        for (size_t i = 0; i < S; i++) capable[S - 1 - i] = raw_capable(c->ops[i]);
+        const std::vector<char> want = raw_stretches(capable);
+        for (size_t i = S; i-- > 0;) {
+            if ((rc = set_raw(want[S - 1 - i]))) return rc;
             if ((rc = undo(i))) return rc;
+        }
     }
     std::vector<double2> sums(uses.size());
     if (!uses.empty()) {

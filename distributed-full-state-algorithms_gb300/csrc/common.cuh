@@ -137,6 +137,20 @@ struct PolDF {  // complex128 storage, double-float arithmetic on the FP32 pipes
     static DEV V mul(K g, V x) { return get(first(g, x)); }
 };
 
+// double-float arithmetic on double-float storage: the same 16 bytes per amplitude
+// hold (re.hi, re.lo, im.hi, im.lo) as floats, so loads and stores skip the IEEE
+// decode and encode.  Only for vectors private to the engine (the backward sweep of
+// a circuit's gradient), converted from and back to IEEE doubles by kernels.
+struct PolDFraw : PolDF {
+    static DEV V load(const store* p, size_t i) {
+        const float4 b = reinterpret_cast<const float4*>(p)[i];
+        return {{b.x, b.y}, {b.z, b.w}};
+    }
+    static DEV void save(store* p, size_t i, V v) {
+        reinterpret_cast<float4*>(p)[i] = make_float4(v.re.hi, v.re.lo, v.im.hi, v.im.lo);
+    }
+};
+
 struct PolF32 {  // complex64 storage and FP32 arithmetic
     using store = float2;
     struct V { float re, im; };

@@ -25,8 +25,9 @@ int fuse_tile_qubits(int precision);
 int fused_run(State* s, const FusedLaunch& a);
 // the backward sweep of a run (operations undone last to first on the state st and the
 // adjoint ad); the run's parametrised gadgets carry gradRow = their order in the sweep,
-// and this CTA's partial sum of gadget p lands in partials[(rowBase + p) * cols + CTA]
+// and this CTA's partial sum of gadget p lands in partials[(rowBase + p) * cols + CTA];
+// raw: both complex128 vectors hold double-float pairs (PolDFraw)
 int fused_run_backward(State* st, State* ad, const FusedLaunch& a, double2* partials, unsigned cols,
-                       unsigned rowBase);
+                       unsigned rowBase, bool raw = false);
 
 }  // namespace dfs

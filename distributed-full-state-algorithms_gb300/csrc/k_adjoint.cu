@@ -86,8 +86,7 @@ struct ConjAcc {
     DEV void add(typename P::V a, typename P::V b, bool neg) { sum_add_conj_prod(s, a, b, neg); }
     DEV typename SumOf<P>::T total() const { return s; }
 };
-template <>
-struct ConjAcc<PolDF> {
+struct ConjAccDF {
     df::acc re, im;
     DEV void zero() { re = {0.f, 0.f}; im = {0.f, 0.f}; }
     DEV void add(PolDF::V a, PolDF::V b, bool neg) {
@@ -97,6 +96,10 @@ struct ConjAcc<PolDF> {
     }
     DEV SumDF total() const { return SumDF{df::acc_result(re), df::acc_result(im)}; }
 };
+template <>
+struct ConjAcc<PolDF> : ConjAccDF {};
+template <>
+struct ConjAcc<PolDFraw> : ConjAccDF {};
 
 // Two consecutive gadgets G2 G1 (X1 != X2, both nonzero) undone in one sweep over both
 // vectors, on the quads {r, r^X1, r^X2, r^X1^X2} of the forward kernel (k_sv.cu
@@ -352,6 +355,15 @@ __global__ void __launch_bounds__(kThreads) k_channel_adj(typename P::store* __r
     }
 }
 
+// ------------------------------------------- IEEE doubles <-> double-float pairs
+// dst may be src: each thread reads an amplitude before it writes it
+template <class PIn, class POut, class IT>
+__global__ void __launch_bounds__(kThreads) k_adj_convert(const typename PIn::store* src, typename POut::store* dst,
+                                                          IT items) {
+    const IT stride = (IT)gridDim.x * kThreads;
+    for (IT j = (IT)blockIdx.x * kThreads + threadIdx.x; j < items; j += stride) POut::save(dst, j, PIn::load(src, j));
+}
+
 // ------------------------------------------------------------ row sums
 // out[r] = sum over the row's cols partials, one warp per row, fixed order.
 __global__ void k_sum_rows(const double2* __restrict__ parts, unsigned rows, unsigned cols,
@@ -379,6 +391,34 @@ static unsigned adj_grid(uint64_t items, int per = 1) {
 }
 unsigned adj_partial_cols() { return (unsigned)ctx().numSMs * kAdjCtasPerSM; }
 
+// F::run for the state's policy, or for PolDFraw when its complex128 vectors hold
+// double-float pairs
+template <class F, class... Args>
+static int dispatch_adj(bool raw, const State* s, Args&&... args) {
+    if (!raw) return dispatch<F>(s, args...);
+    if (s->precision != DFS_C128 || s->forceNative)
+        return fail(DFS_ERR_PRECISION, "double-float pairs need a complex128 state in double-float arithmetic");
+    return wide_index(s) ? F::template run<PolDFraw, uint64_t>(args...) : F::template run<PolDFraw, uint32_t>(args...);
+}
+
+int adj_convert(State* dst, const State* src, bool toRaw) {
+    if (src->precision != DFS_C128 || dst->precision != DFS_C128 || src->forceNative || dst->forceNative ||
+        src->numAmps != dst->numAmps)
+        return fail(DFS_ERR_PRECISION, "double-float pairs need complex128 states of one size");
+    const uint64_t items = src->numAmps;
+    const unsigned grid = adj_grid(items);
+    const double2* in = (const double2*)src->amps;
+    double2* out = (double2*)dst->amps;
+    if (wide_index(src)) {
+        if (toRaw) k_adj_convert<PolDF, PolDFraw, uint64_t><<<grid, kThreads, 0, ctx().stream>>>(in, out, items);
+        else k_adj_convert<PolDFraw, PolDF, uint64_t><<<grid, kThreads, 0, ctx().stream>>>(in, out, items);
+    } else {
+        if (toRaw) k_adj_convert<PolDF, PolDFraw, uint32_t><<<grid, kThreads, 0, ctx().stream>>>(in, out, (uint32_t)items);
+        else k_adj_convert<PolDFraw, PolDF, uint32_t><<<grid, kThreads, 0, ctx().stream>>>(in, out, (uint32_t)items);
+    }
+    return check_launch("double-float conversion");
+}
+
 struct RunAdjGadget {
     template <class P, class IT>
     static int run(State* st, State* ad, uint64_t mX, uint64_t mYZ, int numY, double phi, double2* row) {
@@ -399,8 +439,9 @@ struct RunAdjGadget {
         return check_launch("adjoint gadget");
     }
 };
-int adj_gadget_step(State* st, State* ad, uint64_t maskX, uint64_t maskYZ, int numY, double phi, double2* row) {
-    return dispatch<RunAdjGadget>(st, st, ad, maskX, maskYZ, numY, phi, row);
+int adj_gadget_step(State* st, State* ad, uint64_t maskX, uint64_t maskYZ, int numY, double phi, double2* row,
+                    bool raw) {
+    return dispatch_adj<RunAdjGadget>(raw, st, st, ad, maskX, maskYZ, numY, phi, row);
 }
 
 struct RunAdjTwoGadgets {
@@ -432,9 +473,9 @@ struct RunAdjTwoGadgets {
     }
 };
 int adj_two_gadgets_step(State* st, State* ad, const GadgetSpec& g1, const GadgetSpec& g2, double2* row1,
-                         double2* row2) {
+                         double2* row2, bool raw) {
     if (g1.x == 0 || g2.x == 0 || g1.x == g2.x) return fail(DFS_ERR_INVALID_ARG, "two gadgets need distinct X parts");
-    return dispatch<RunAdjTwoGadgets>(st, st, ad, g1, g2, row1, row2);
+    return dispatch_adj<RunAdjTwoGadgets>(raw, st, st, ad, g1, g2, row1, row2);
 }
 
 struct RunPauliSumApply {
@@ -494,8 +535,9 @@ struct RunChannelAdj {
         return go<P, IT, 2>(ad, rho, nullptr, *m2, row);
     }
 };
-int adj_channel_step(State* ad, const State* rho, const ChannelMats<1>* m1, const ChannelMats<2>* m2, double2* row) {
-    return dispatch<RunChannelAdj>(ad, ad, rho, m1, m2, row);
+int adj_channel_step(State* ad, const State* rho, const ChannelMats<1>* m1, const ChannelMats<2>* m2, double2* row,
+                     bool raw) {
+    return dispatch_adj<RunChannelAdj>(raw, ad, ad, rho, m1, m2, row);
 }
 
 int adj_sum_rows(const double2* parts, unsigned rows, unsigned cols, double2* out, cudaStream_t stream) {

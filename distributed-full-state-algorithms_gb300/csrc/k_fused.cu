@@ -207,8 +207,12 @@ static int launch_fused_bwd(State* st, State* ad, const FusedLaunch& a, double2*
 }
 
 int fused_run_backward(State* st, State* ad, const FusedLaunch& a, double2* partials, unsigned cols,
-                       unsigned rowBase) {
+                       unsigned rowBase, bool raw) {
     if (a.m < 4 || a.m > (unsigned)kFuseMaxTileQubits - 1) return fail(DFS_ERR_INVALID_ARG, "tile of %u qubits", a.m);
+    if (raw) {
+        if (st->precision != DFS_C128) return fail(DFS_ERR_PRECISION, "double-float pairs need a complex128 state");
+        return launch_fused_bwd<PolDFraw, PolDFsm>(st, ad, a, partials, cols, rowBase);
+    }
     switch (st->precision) {
         case DFS_C128: return launch_fused_bwd<PolDF, PolDFsm>(st, ad, a, partials, cols, rowBase);
         case DFS_C128_NATIVE: return launch_fused_bwd<PolF64, PolF64>(st, ad, a, partials, cols, rowBase);

@@ -123,6 +123,51 @@ def test_density_matrix_channels_and_gadgets(dfs, oracle, prec, rng):
         assert abs(grad[i] - ref[i]) <= tol * max(1.0, abs(ref[i])), (i, k, grad[i], ref[i])
 
 
+def _gadgets(rng, n, count):
+    G = circuits.Gate
+    out = []
+    for _ in range(count):
+        t, p = circuits.random_pauli_string(rng, n, int(rng.integers(2, 4)))
+        out.append(G("pauli_gadget", t, paulis=p, param=float(rng.normal())))
+    return out
+
+
+@pytest.mark.parametrize("form", ["sv_fused", "sv_unfused", "dm"])
+def test_double_float_stretches(dfs, oracle, form, rng):
+    """Complex128 backward sweeps hold both vectors as double-float pairs over long
+    stretches of gadget, channel and fused steps and as IEEE doubles around other
+    operations.  The sweep here (the circuit read backwards) enters and leaves that
+    form twice, ends in it, and for the density matrix restores a checkpoint inside a
+    stretch."""
+    G = circuits.Gate
+    dm = form == "dm"
+    n = 4 if dm else 7
+    if dm:
+        gates = (_gadgets(rng, n, 5) + [G("one_targ", (1,), matrix=haar(rng, 2))] + _gadgets(rng, n, 4) +
+                 [G("depol1", (2,), param=0.06)] + _gadgets(rng, n, 4) + [G("swap", (0, 3))] +
+                 _gadgets(rng, n, 9) + [G("damping", (1,), param=0.05)])
+    else:
+        gates = (_gadgets(rng, n, 5) + [G("ctrl", (4,), controls=(1,), matrix=haar(rng, 2))] +
+                 _gadgets(rng, n, 9) + [G("phase_gadget", (0, 5), param=0.3), G("phase_gadget", (2,), param=-0.8)] +
+                 [G("one_targ", (6,), matrix=haar(rng, 2))] + _gadgets(rng, n, 10))
+    coeffs, paulis = circuits.pauli_sum(n, 8, seed=int(rng.integers(1 << 30)))
+    a0 = ginibre_dm(rng, n) if dm else gaussian_state(rng, 1 << n, normalise=True)
+    circ, params = circuits.record(dfs, n, gates, density_matrix=dm)
+    circ.fusion = form == "sv_fused"
+    init = _dm(dfs, n, "c128", a0) if dm else _sv(dfs, n, "c128", a0)
+    circ.expectation(init, params, coeffs, paulis)
+    grad = circ.gradient(params)
+    ref = reference_gradient(oracle, gates, params, a0, coeffs, paulis, dm=dm)
+    kinds = [g.kind for g in gates if g.kind in circuits.PARAM_KINDS]
+    for i, k in enumerate(kinds):
+        tol = GRAD_TOL["c128"] if k.endswith("gadget") else FD_TOL
+        assert abs(grad[i] - ref[i]) <= tol * max(1.0, abs(ref[i])), (i, k, grad[i], ref[i])
+    # a second expectation and gradient on the same circuit: the vectors the sweep left
+    # as double-float pairs are rewritten
+    circ.expectation(init, params, coeffs, paulis)
+    _check(circ.gradient(params), ref, GRAD_TOL["c128"] if not dm else FD_TOL)
+
+
 def test_torch_autograd(dfs, oracle, rng):
     torch = pytest.importorskip("torch")
     n = 6
