@@ -555,8 +555,14 @@ int dfs_batch_get_state(dfs_batch b, unsigned index, dfs_state out) {
     if (rc) return rc;
     range_forget(out);
     State v = arena_view(b, 1, index);
-    cudaError_t e = cudaMemcpyAsync(out->amps, v.amps, v.numAmps * elem_bytes(b->precision),
-                                    cudaMemcpyDeviceToDevice, ctx().stream);
+    cudaError_t e = cudaSuccess;
+    if (b->precision == DFS_C128) {
+        // complex128 working states hold double-float pairs (PolDFraw in k_batch)
+        if ((rc = adj_convert(out, &v, false))) return rc;
+    } else {
+        e = cudaMemcpyAsync(out->amps, v.amps, v.numAmps * elem_bytes(b->precision), cudaMemcpyDeviceToDevice,
+                            ctx().stream);
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx().stream);
     return e == cudaSuccess ? DFS_SUCCESS : cuda_fail(e, "batch state copy");
 }

@@ -140,15 +140,20 @@ struct PolDF {  // complex128 storage, double-float arithmetic on the FP32 pipes
 // double-float arithmetic on double-float storage: the same 16 bytes per amplitude
 // hold (re.hi, re.lo, im.hi, im.lo) as floats, so loads and stores skip the IEEE
 // decode and encode.  Only for vectors private to the engine (the backward sweep of
-// a circuit's gradient), converted from and back to IEEE doubles by kernels.
+// a circuit's gradient, the working states of a batch), converted from and back to
+// IEEE doubles by kernels.  A store type of its own, so that the kernels that move
+// stored words without decoding them (swaps, Pauli tensors) pick the matching sign
+// flips.
+struct alignas(16) DFPair {
+    df::f2 re, im;
+};
 struct PolDFraw : PolDF {
+    using store = DFPair;
     static DEV V load(const store* p, size_t i) {
-        const float4 b = reinterpret_cast<const float4*>(p)[i];
-        return {{b.x, b.y}, {b.z, b.w}};
+        const DFPair w = p[i];
+        return {w.re, w.im};
     }
-    static DEV void save(store* p, size_t i, V v) {
-        reinterpret_cast<float4*>(p)[i] = make_float4(v.re.hi, v.re.lo, v.im.hi, v.im.lo);
-    }
+    static DEV void save(store* p, size_t i, V v) { p[i] = DFPair{v.re, v.im}; }
 };
 
 struct PolF32 {  // complex64 storage and FP32 arithmetic

@@ -402,18 +402,20 @@ static int dispatch_adj(bool raw, const State* s, Args&&... args) {
 }
 
 int adj_convert(State* dst, const State* src, bool toRaw) {
-    if (src->precision != DFS_C128 || dst->precision != DFS_C128 || src->forceNative || dst->forceNative ||
-        src->numAmps != dst->numAmps)
+    if (src->precision != DFS_C128 || dst->precision != DFS_C128 || src->numAmps != dst->numAmps)
         return fail(DFS_ERR_PRECISION, "double-float pairs need complex128 states of one size");
     const uint64_t items = src->numAmps;
     const unsigned grid = adj_grid(items);
-    const double2* in = (const double2*)src->amps;
-    double2* out = (double2*)dst->amps;
-    if (wide_index(src)) {
-        if (toRaw) k_adj_convert<PolDF, PolDFraw, uint64_t><<<grid, kThreads, 0, ctx().stream>>>(in, out, items);
-        else k_adj_convert<PolDFraw, PolDF, uint64_t><<<grid, kThreads, 0, ctx().stream>>>(in, out, items);
+    const bool wide = wide_index(src);
+    if (toRaw) {
+        const double2* in = (const double2*)src->amps;
+        DFPair* out = (DFPair*)dst->amps;
+        if (wide) k_adj_convert<PolDF, PolDFraw, uint64_t><<<grid, kThreads, 0, ctx().stream>>>(in, out, items);
+        else k_adj_convert<PolDF, PolDFraw, uint32_t><<<grid, kThreads, 0, ctx().stream>>>(in, out, (uint32_t)items);
     } else {
-        if (toRaw) k_adj_convert<PolDF, PolDFraw, uint32_t><<<grid, kThreads, 0, ctx().stream>>>(in, out, (uint32_t)items);
+        const DFPair* in = (const DFPair*)src->amps;
+        double2* out = (double2*)dst->amps;
+        if (wide) k_adj_convert<PolDFraw, PolDF, uint64_t><<<grid, kThreads, 0, ctx().stream>>>(in, out, items);
         else k_adj_convert<PolDFraw, PolDF, uint32_t><<<grid, kThreads, 0, ctx().stream>>>(in, out, (uint32_t)items);
     }
     return check_launch("double-float conversion");

@@ -11,6 +11,7 @@
 // other waiter also watches, so the launch always ends.  The launch is cooperative,
 // so all teams are resident at once.
 #include <cmath>
+#include <type_traits>
 
 #include "batch.hpp"
 #include "kernels.cuh"
@@ -208,12 +209,18 @@ template <class P>
 DEV bool run_circuit(const Args& a, const CircD& c, unsigned rank, TeamSync* ts, unsigned& gen) {
     using S = typename P::store;
     __shared__ typename P::K sG[64];
-    S* init = (S*)a.init + c.off;
     S* psi = (S*)a.psi + c.off;
     S* lam = (S*)a.lam + c.off;
     const IT N = (IT)1 << c.n;
     const Span sp{(IT)rank * kThreads + threadIdx.x, (IT)a.width * kThreads};
-    for (IT j = sp.first; j < N; j += sp.stride) psi[j] = init[j];
+    if constexpr (std::is_same_v<P, PolDFraw>) {
+        // the working state holds double-float pairs; the initial states are IEEE doubles
+        const double2* in = (const double2*)a.init + c.off;
+        for (IT j = sp.first; j < N; j += sp.stride) P::save(psi, j, PolDF::load(in, j));
+    } else {
+        const S* init = (const S*)a.init + c.off;
+        for (IT j = sp.first; j < N; j += sp.stride) psi[j] = init[j];
+    }
     if (!team_sync(a, ts, gen)) return false;
     for (unsigned o = c.opBegin; o < c.opEnd; o++) {
         forward_op<P>(a, a.ops[o], psi, N, sp, sG);
@@ -279,7 +286,7 @@ static cudaError_t launch_p(const Args& a, unsigned grid, cudaStream_t stream) {
 int launch(int precision, const Args& a, unsigned grid, cudaStream_t stream) {
     cudaError_t e;
     switch (precision) {
-        case DFS_C128: e = launch_p<PolDF>(a, grid, stream); break;
+        case DFS_C128: e = launch_p<PolDFraw>(a, grid, stream); break;
         case DFS_C128_NATIVE: e = launch_p<PolF64>(a, grid, stream); break;
         case DFS_C64: e = launch_p<PolF32>(a, grid, stream); break;
         default: return fail(DFS_ERR_PRECISION, "unknown precision %d", precision);
@@ -290,7 +297,7 @@ int launch(int precision, const Args& a, unsigned grid, cudaStream_t stream) {
 int max_ctas_per_sm(int precision, int* out) {
     cudaError_t e;
     switch (precision) {
-        case DFS_C128: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_batch<PolDF>, kThreads, 0); break;
+        case DFS_C128: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_batch<PolDFraw>, kThreads, 0); break;
         case DFS_C128_NATIVE:
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_batch<PolF64>, kThreads, 0);
             break;

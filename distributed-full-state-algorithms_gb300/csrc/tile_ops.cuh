@@ -15,6 +15,12 @@ namespace dfs {
 // raw-storage forms of kernels.cuh, for amplitudes held decoded in shared memory)
 DEV PolDF::V raw_neg(PolDF::V v) { return {df::neg(v.re), df::neg(v.im)}; }
 DEV PolDF::V raw_rot(PolDF::V v, int k, int s) { return rot<PolDF>(v, k, s); }
+// the same for amplitudes stored as double-float pairs (PolDFraw)
+DEV DFPair raw_neg(DFPair v) { return {df::neg(v.re), df::neg(v.im)}; }
+DEV DFPair raw_rot(DFPair v, int k, int s) {
+    const PolDF::V r = rot<PolDF>(PolDF::V{v.re, v.im}, k, s);
+    return {r.re, r.im};
+}
 
 namespace batch {
 
