@@ -16,6 +16,7 @@
 
 #include "adjoint.hpp"
 #include "kernels.cuh"
+#include "pauli_sum.cuh"
 #include "reduce.cuh"
 
 namespace dfs {
@@ -223,18 +224,7 @@ __global__ void __launch_bounds__(kThreads) k_pauli_sum_apply(const typename P::
     sum_zero(s);
     const IT stride = (IT)gridDim.x * kThreads;
     for (IT j = (IT)blockIdx.x * kThreads + threadIdx.x; j < items; j += stride) {
-        typename P::A acc;
-        for (unsigned t = 0; t < numTerms; t++) {
-            const AdjTerm tm = ts[t];
-            IT src = j ^ (IT)tm.x;
-            typename P::V v = rot<P>(P::load(psi, src), tm.powY, parity(src & (IT)tm.yz));
-            typename P::R c;
-            if constexpr (P::kEmulated) c = df::f2{tm.cHi, tm.cLo};
-            else c = (typename P::R)tm.c;
-            if (t == 0) acc = P::first_r(c, v);
-            else P::mac_r(acc, c, v);
-        }
-        typename P::V r = P::get(acc);
+        const typename P::V r = pauli_sum_at<P>(psi, j, ts, numTerms);
         P::save(out, j, r);
         sum_add_conj_prod(s, P::load(psi, j), r, false);
     }

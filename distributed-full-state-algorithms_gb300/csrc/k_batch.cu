@@ -15,6 +15,7 @@
 
 #include "batch.hpp"
 #include "kernels.cuh"
+#include "pauli_sum.cuh"
 #include "tc.cuh"
 #include "reduce.cuh"
 #include "tile_ops.cuh"
@@ -186,18 +187,7 @@ __device__ __noinline__ void hamiltonian(const Args& a, const CircD& c, const ty
     Sum s;
     sum_zero(s);
     for (IT j = sp.first; j < N; j += sp.stride) {
-        typename P::A acc;
-        for (unsigned t = 0; t < T; t++) {
-            const AdjTerm tm = sT[t];
-            IT src = j ^ (IT)tm.x;
-            typename P::V v = rot<P>(P::load(x, src), tm.powY, parity(src & (IT)tm.yz));
-            typename P::R cf;
-            if constexpr (P::kEmulated) cf = df::f2{tm.cHi, tm.cLo};
-            else cf = (typename P::R)tm.c;
-            if (t == 0) acc = P::first_r(cf, v);
-            else P::mac_r(acc, cf, v);
-        }
-        typename P::V r = P::get(acc);
+        const typename P::V r = pauli_sum_at<P>(x, j, sT, T);
         P::save(l, j, r);
         sum_add_conj_prod(s, P::load(x, j), r, false);
     }
