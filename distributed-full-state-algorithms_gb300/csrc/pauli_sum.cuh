@@ -34,6 +34,16 @@ DEV typename P::V term_value(const typename P::store* psi, IT j, const AdjTerm& 
 template <class P, class IT>
 DEV typename P::V pauli_sum_at(const typename P::store* psi, IT j, const AdjTerm* ts, unsigned T) {
     constexpr int U = term_loads<P>();
+    if constexpr (U == 1) {
+        typename P::A acc;
+        for (unsigned t = 0; t < T; t++) {
+            const AdjTerm tm = ts[t];
+            const typename P::V v = term_value<P>(psi, j, tm);
+            if (t == 0) acc = P::first_r(term_coeff<P>(tm), v);
+            else P::mac_r(acc, term_coeff<P>(tm), v);
+        }
+        return P::get(acc);
+    }
     typename P::A acc = P::first_r(term_coeff<P>(ts[0]), term_value<P>(psi, j, ts[0]));
     unsigned t = 1;
     for (; t + U <= T; t += U) {
