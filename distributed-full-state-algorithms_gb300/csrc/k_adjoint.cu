@@ -114,7 +114,9 @@ struct AdjTwoGadgetOp {
 };
 
 // three CTAs per SM (80 registers, a few spilled): the 11-qubit density-matrix ansatz's
-// backward 40.1 -> 38.0 ms with the Dot2 sums, the 24-qubit complex128 one 3% faster
+// backward 40.1 -> 38.0 ms with the Dot2 sums, the 24-qubit complex128 one 3% faster; on
+// double-float pairs two CTAs per SM (128 registers) measured 47.7 -> 49.4 ms for the
+// 24-qubit backward, and four spill over 100 bytes
 // kOdd1, kOdd2: the parities of m1, m2 (fixed re/im swaps, as in k_two_gadgets)
 template <class P, class IT, int kOdd1, int kOdd2>
 __global__ void __launch_bounds__(kThreads, 3) k_adj_two_gadgets(typename P::store* __restrict__ st,
